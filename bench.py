@@ -1,0 +1,412 @@
+"""Benchmark: 2048^2 complex64 angular-spectrum propagates/s on one GB300.
+
+Workload (``config.workload``): Gaussian beam, npoints=2048, area 2 mm,
+wl 632 nm, waist 100 um, complex64, propagated by z = 1 cm per step.  A step
+is one fused field -> field propagate (fft2 -> H(z) in registers -> ifft2,
+read field / write field) with the field resident in HBM; the L2 is flushed
+(a 320 MiB write) before every timed step and the flush is outside the timed
+events.
+
+Also reported: the Beam2D.propagate steady state (stored spectrum -> field),
+the plain unfused form (fft2, H grid in HBM, multiply, ifft2) with the
+float-float H and with the reference-literal FP64 H, the plain-FP32-phase
+variant's error, an N sweep (512..4096) and ``e2e``: the same step through
+the C ABI with host buffers (pinned H2D copy, propagate, D2H copy timed).
+
+``--impl reference`` times the reference algorithm (the numpy oracle port of
+beam2d.py:481-490 with the fft2 of the field first) on the host cores, one
+process per core, on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_HEAD, AREA, WL, WAIST, Z = 2048, 0.2, 632e-7, 100e-4, 1.0
+METRIC = "2048^2 complex64 fused field->field propagates/s"
+UNIT = "propagates/s"
+WORKLOAD = "gaussian beam 2048^2, area 2 mm, wl 632 nm, waist 100 um, complex64, z=1 cm/step"
+
+
+# ----------------------------------------------------------------- CPU side --
+def _cpu_worker_init(n, area, wl):
+    global _W
+    import numpy as _np
+    from oracle import lp_oracle as O
+    g = O.grids(area, n, wl)
+    f = O.gaussian(n, area, 1.0, WAIST).astype(_np.complex64)
+    _W = (g["Kz"], f)
+
+
+def _cpu_worker_step(z):
+    """One field -> field propagate exactly as the reference computes it:
+    spectrum = fft2(field) (beam2d.py:217), spectrum *= H (:485-489),
+    field = ifft2(spectrum) (:490), complex64 arrays, FP64 phase."""
+    import numpy as _np
+    from oracle import lp_oracle as O
+    Kz, f = _W
+    t0 = time.perf_counter()
+    s = _np.fft.fft2(f)
+    s, out = O.propagate(s, Kz, z)
+    dt = time.perf_counter() - t0
+    return dt, float(_np.abs(out[0, 0]))
+
+
+def cpu_baseline(steps: int, n=N_HEAD, procs=None):
+    """Run `steps` rounds; each round every process propagates one beam."""
+    procs = procs or os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs, initializer=_cpu_worker_init, initargs=(n, AREA, WL)) as pool:
+        pool.map(_cpu_worker_step, [Z] * procs)  # warm-up
+        walls = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            pool.map(_cpu_worker_step, [Z] * procs)
+            walls.append(time.perf_counter() - t0)
+    total = procs * steps
+    return dict(value=total / sum(walls), unit=UNIT, cores=procs, kind="port",
+                sample=f"{total} field->field propagates at {n}^2 complex64 "
+                       f"({procs} processes x {steps} rounds, numpy pocketfft)")
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    steps = max(1, min(args.steps, 10))
+    cb = cpu_baseline(steps)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
+        "n_gpus": args.gpus, "steps": steps, "warmup": 1,
+        "ms_per_step": 1000.0 / cb["value"] * cb["cores"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "flush_l2": False},
+        "cpu_baseline": cb,
+        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ----------------------------------------------------------------- GPU side --
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,"
+         "utilization.gpu")
+
+    def __init__(self, index):
+        self.index, self.samples, self.windows = index, [], []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append((time.time(), [s.strip() for s in line.split(",")]))
+
+    def window(self):
+        return _Window(self)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        inside = [s for t, s in self.samples
+                  if any(a - 0.15 <= t <= b + 0.15 for a, b in self.windows)]
+        use = inside or [s for _, s in self.samples]
+        if not use:
+            return None
+        mhz = [float(s[1]) for s in use if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in use if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in use for i in range(4)
+                          if len(s) > 5 + i and s[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(mhz) if mhz else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(use), "in_timed_region": bool(inside)}
+
+
+class _Window:
+    def __init__(self, cs):
+        self.cs = cs
+
+    def __enter__(self):
+        self.t0 = time.time()
+
+    def __exit__(self, *a):
+        self.cs.windows.append((self.t0, time.time()))
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d["hbm_gbs"], "measured"
+    return 6800.0, "fallback"
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--quick", action="store_true", help="skip the sweep")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    # CPU baseline first (spawned pool, before any CUDA work in this process).
+    cb = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cb = cpu_baseline(steps=3)
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from lightprop2d_gb300 import _lib as L
+    from lightprop2d_gb300 import backend as B
+    from oracle import lp_oracle as O
+    lib = L.load()
+    B.init(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    flush = torch.empty(320 * 2 ** 20 // 4, dtype=torch.float32, device=dev)
+
+    def vp(t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    nul = ctypes.c_void_p(0)
+
+    def fused(n, fin, fout, z=Z, flags=0):
+        return lib.lp_propagate_field(vp(fin), vp(fout), nul, nul, n, AREA, WL, z, 0.0,
+                                      nul, 0, nul, 0, flags, sp)
+
+    def spec_state(n, s, fout, z=Z):
+        return lib.lp_propagate(vp(s), vp(fout), n, AREA, WL, z, nul, 0,
+                                L.LP_FLAG_SPECTRUM_READONLY, sp)
+
+    def plain(n, fin, fout, fp64=False):
+        return lib.lp_plain_propagate_field(vp(fin), vp(fout), n, AREA, WL, Z,
+                                            L.LP_FLAG_PLAIN_FP64_H if fp64 else 0, sp)
+
+    def make(n):
+        f = torch.as_tensor(O.gaussian(n, AREA, 1.0, WAIST).astype(np.complex64), device=dev)
+        return f, torch.empty_like(f)
+
+    def timed(fn, steps, warmup, npass):
+        """Per-step CUDA-event timing with an L2 flush before each step.
+        Returns (step_ms list, per-pass ms lists)."""
+        for _ in range(warmup):
+            L.check(fn(), "warm-up")
+        torch.cuda.synchronize()
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(npass + 1)]
+               for _ in range(steps)]
+        for row in evs:
+            for e in row:
+                e.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        for i in range(steps):
+            flush.fill_(float(i))
+            arr = (ctypes.c_void_p * (npass + 1))(*[e.cuda_event for e in evs[i]])
+            lib.lp_profile_events(arr, npass + 1)
+            L.check(fn(), "timed step")
+        lib.lp_profile_events(None, 0)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        step = [row[0].elapsed_time(row[-1]) for row in evs]
+        passes = [[row[p].elapsed_time(row[p + 1]) for row in evs] for p in range(npass)]
+        return step, passes
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+
+    # ---------------------------------------------------------- headline --
+    n = N_HEAD
+    fin, fout = make(n)
+    with clocks.window():
+        step_ms, pass_ms = timed(lambda: fused(n, fin, fout), args.steps, args.warmup, 3)
+    tot_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([tot_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_ms = float(t)
+    ms_step = tot_ms / args.steps
+    value = world * args.steps / (tot_ms / 1e3)
+
+    # parity of the timed result vs the oracle (same step, complex128)
+    g = O.grids(AREA, n, WL)
+    _, f_ref = O.propagate(np.fft.fft2(O.gaussian(n, AREA, 1.0, WAIST)), g["Kz"], Z)
+    torch.cuda.synchronize()
+    err = O.rel_l2(fout.cpu().numpy(), f_ref)
+    eerr = O.energy_err(fout.cpu().numpy(), f_ref)
+
+    hbm, peak_kind = peaks()
+    pass_avg = [statistics.fmean(p) for p in pass_ms]
+    names = ["row_fwd", "col_fwd_H_inv", "row_inv"]
+    dom = int(np.argmax(pass_avg))
+    alg_bytes = 16 * n * n  # each pass reads and writes one complex64 grid
+    achieved = alg_bytes / (pass_avg[dom] * 1e-3) / 1e9
+    step_gbs = alg_bytes / (ms_step * 1e-3) / 1e9
+
+    extra = {"passes_ms": dict(zip(names, [round(x, 5) for x in pass_avg])),
+             "step_effective_gbs": round(step_gbs, 1),
+             "step_roofline_frac": round(step_gbs / hbm, 4),
+             "rel_l2_vs_fp64_oracle": err, "energy_err": eerr}
+
+    # ------------------------------------------------------------ variants --
+    if rank == 0 and not args.quick:
+        ks = max(10, min(200, args.steps // 10))
+        with clocks.window():
+            s = B.fft2(fin)
+            st_ms, st_pass = timed(lambda: spec_state(n, s, fout), ks, 3, 2)
+
+        # plain paths have no pass events; time them whole
+        def whole(fn, steps, warm=3):
+            for _ in range(warm):
+                L.check(fn(), "warm-up")
+            torch.cuda.synchronize()
+            out = []
+            for i in range(steps):
+                flush.fill_(float(i))
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                L.check(fn(), "plain step")
+                b.record(stream)
+                out.append((a, b))
+            torch.cuda.synchronize()
+            return [a.elapsed_time(b) for a, b in out]
+        with clocks.window():
+            pl = whole(lambda: plain(n, fin, fout), ks)
+            pl64 = whole(lambda: plain(n, fin, fout, fp64=True), max(5, ks // 4))
+        torch.cuda.synchronize()
+        # FP32-phase vs float-float phase error at every z of the workload
+        f0 = O.gaussian(n, AREA, 1.0, WAIST)
+        s0 = torch.as_tensor(np.fft.fft2(f0).astype(np.complex64), device=dev)
+        zerr = {}
+        for z in (0.1, 1.0, 5.0, 10.0, 50.0):
+            _, fr = O.propagate(np.fft.fft2(f0), g["Kz"], z)
+            a = B.propagate(s0, AREA, WL, z, write_spectrum=False)
+            b = B.propagate(s0, AREA, WL, z, write_spectrum=False, flags=L.LP_FLAG_PHASE_FP32)
+            torch.cuda.synchronize()
+            zerr[str(z)] = {"ff_phase": O.rel_l2(a.cpu().numpy(), fr),
+                            "fp32_phase": O.rel_l2(b.cpu().numpy(), fr)}
+        sweep = {}
+        for nn in (512, 1024, 2048, 4096):
+            a_in, a_out = make(nn)
+            with clocks.window():
+                sm, _ = timed(lambda: fused(nn, a_in, a_out), ks, 3, 3)
+            ms = statistics.fmean(sm)
+            sweep[str(nn)] = {"ms": round(ms, 5), "propagates_per_s": round(1e3 / ms, 1),
+                              "effective_gbs": round(16 * nn * nn / (ms * 1e-3) / 1e9, 1)}
+            del a_in, a_out
+        st = statistics.fmean(st_ms)
+        extra.update({
+            "spectrum_state_propagate": {
+                "ms": round(st, 5), "propagates_per_s": round(1e3 / st, 1),
+                "effective_gbs": round(16 * n * n / (st * 1e-3) / 1e9, 1),
+                "passes_ms": [round(statistics.fmean(p), 5) for p in st_pass]},
+            "plain_unfused": {"ms": round(statistics.fmean(pl), 5),
+                              "propagates_per_s": round(1e3 / statistics.fmean(pl), 1),
+                              "fused_speedup": round(statistics.fmean(pl) / ms_step, 3)},
+            "plain_unfused_fp64_h": {"ms": round(statistics.fmean(pl64), 5),
+                                     "fused_speedup": round(statistics.fmean(pl64) / ms_step, 3)},
+            "phase_error_by_z": zerr, "sweep": sweep})
+
+    # ----------------------------------------------------------------- e2e --
+    hin = torch.empty((n, n), dtype=torch.complex64, pin_memory=True)
+    hin.copy_(torch.as_tensor(O.gaussian(n, AREA, 1.0, WAIST).astype(np.complex64)))
+    hout = torch.empty_like(hin).pin_memory()
+    ke = max(5, min(100, args.steps // 20))
+    e2e_ms = []
+    with clocks.window():
+        for i in range(ke + 3):
+            flush.fill_(float(i))
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fin.copy_(hin, non_blocking=True)
+            L.check(fused(n, fin, fout), "e2e step")
+            hout.copy_(fout, non_blocking=True)
+            b.record(stream)
+            if i >= 3:
+                e2e_ms.append((a, b))
+        torch.cuda.synchronize()
+    e2e_t = statistics.fmean([a.elapsed_time(b) for a, b in e2e_ms])
+    clocks.stop()
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "flush_l2": True, "flush_bytes": 320 * 2 ** 20,
+                       "parallelism": f"replicas{world}"},
+            "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1),
+                         "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
+                         "frac": round(achieved / hbm, 4), "traffic": None,
+                         "alg_bytes_per_launch": alg_bytes},
+            "cpu_baseline": cb,
+            "e2e": {"value": world * 1e3 / e2e_t, "unit": UNIT,
+                    "h2d_bytes_per_step": 8 * n * n, "d2h_bytes_per_step": 8 * n * n},
+            "clocks": clocks.summary(),
+            "gpu_launches": 3 * args.steps,
+            **extra,
+        }
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

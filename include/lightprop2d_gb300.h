@@ -1,0 +1,174 @@
+/*
+ * lightprop2d_gb300.h -- C ABI of the GB300 (sm_103a) angular-spectrum backend.
+ *
+ * Every entry point maps one operation of lightprop2d's Beam2D
+ * (lightprop2d/beam2d.py, version 1.0.4) onto hand-written CUDA kernels.
+ *
+ *   - All array arguments are DEVICE pointers to row-major N x N grids,
+ *     index [iy * N + ix], iy <-> Y (rows), ix <-> X (columns), exactly the
+ *     layout of Beam2D.field / Beam2D.spectrum (beam2d.py:299-308).
+ *   - Complex data is interleaved complex64 (numpy / torch complex64 layout).
+ *   - Spectra use the unshifted fftfreq order (DC at index 0).
+ *   - Lengths are in centimetres, like the reference (beam2d.py:37-41).
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *     asynchronous with respect to the host; results are ready once the
+ *     stream reaches them.
+ *   - Ownership: the caller owns every buffer passed in.  The library keeps
+ *     per-device twiddle tables (static device arrays) and a per-(device,
+ *     stream) scratch grid that lp_workspace_release() frees.
+ *   - Errors: every call returns an lp_status; no exception crosses the ABI.
+ *     lp_last_error() returns a thread-local message for the last failure.
+ *   - Supported N: powers of two from 16 to 4096.  Other N return
+ *     LP_ERR_UNSUPPORTED_SIZE (the reference accepts any N through numpy).
+ *   - Pointers must be 8-byte aligned (complex64); N >= 16 keeps every row
+ *     16-byte aligned when the base pointer is.
+ */
+#ifndef LIGHTPROP2D_GB300_H
+#define LIGHTPROP2D_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LP_ABI_VERSION 1
+
+typedef struct lp_cfloat {
+  float re;
+  float im;
+} lp_cfloat;
+
+typedef enum lp_status {
+  LP_OK = 0,
+  LP_ERR_INVALID_ARGUMENT = 1,  /* null pointer, bad dtype code, non-finite scalar */
+  LP_ERR_UNSUPPORTED_SIZE = 2,  /* N not a power of two in [16, 4096] */
+  LP_ERR_MISALIGNED = 3,        /* pointer not 8-byte aligned */
+  LP_ERR_CUDA = 4,              /* a CUDA runtime call failed (see lp_last_error) */
+  LP_ERR_OUT_OF_MEMORY = 5,     /* scratch allocation failed */
+  LP_ERR_NOT_INITIALIZED = 6,   /* first use on a device inside stream capture */
+  LP_ERR_TIMEOUT = 7,           /* a bounded device-side wait gave up (batched queue) */
+  LP_ERR_INTERNAL = 8
+} lp_status;
+
+/* Element type of an optional mask argument. */
+typedef enum lp_mask_type {
+  LP_MASK_NONE = 0,
+  LP_MASK_F32 = 1,        /* real float32 multiplier */
+  LP_MASK_C64 = 2,        /* complex64 multiplier */
+  LP_MASK_U8 = 3,         /* bool / uint8 (0 or 1) */
+  LP_MASK_PHASE_F32 = 4,  /* float32 phase phi in radians: multiplier exp(i*phi) */
+  LP_MASK_F64 = 5,        /* real float64 multiplier (numpy default dtype) */
+  LP_MASK_C128 = 6        /* complex128 multiplier, rounded to complex64 */
+} lp_mask_type;
+
+/* Flags (bitwise OR). */
+#define LP_FLAG_PHASE_FP32 0x1u         /* transfer phase kz*z in plain FP32 (comparison variant) */
+#define LP_FLAG_EVANESCENT_MASK 0x2u    /* H = 0 where kx^2+ky^2 > k0^2 (reference: H = 1) */
+#define LP_FLAG_ADJOINT 0x4u            /* conjugate every multiplier: the adjoint operator */
+#define LP_FLAG_SPECTRUM_READONLY 0x8u  /* lp_propagate: do not write spectrum*H back */
+#define LP_FLAG_DZ 0x10u                /* multiply the spectrum by -2*pi*i*kz as well (d/dz) */
+
+/* ---------------------------------------------------------------- meta -- */
+int lp_abi_version(void);
+const char* lp_last_error(void);
+const char* lp_status_string(int status);
+/* 1 when N is supported, else 0. */
+int lp_is_supported_n(int n);
+/* One-time per-device set-up (twiddle tables).  Called implicitly by the
+ * first entry point on a device; call it explicitly before capturing any of
+ * these calls into a CUDA graph. */
+lp_status lp_init(int device);
+/* Frees every cached scratch grid (all devices and streams). */
+lp_status lp_workspace_release(void);
+/* Measurement hook (no counterpart in the reference): until called again with
+ * count = 0, lp_propagate_field and lp_propagate record the caller's CUDA
+ * events (cudaEvent_t, created on the current device) on their stream at the
+ * pass boundaries of each call: events[0] before the first pass and
+ * events[i] after pass i (3 passes for lp_propagate_field, 2 for
+ * lp_propagate).  Thread-local. */
+lp_status lp_profile_events(void** events, int count);
+
+/* ------------------------------------------------------------ transforms --
+ * numpy convention: forward unnormalised, inverse scaled by 1/N^2.
+ * Replaces Beam2D._fft2 / Beam2D._ifft2 (beam2d.py:207-229).
+ * in == out is allowed. */
+lp_status lp_fft2(const lp_cfloat* in, lp_cfloat* out, int n, int inverse,
+                  void* stream);
+
+/* -------------------------------------------------------------- propagate --
+ * Beam2D.propagate(z) (beam2d.py:462-490) on the stored spectrum:
+ *     spectrum *= kmask * H(z)         (written back unless SPECTRUM_READONLY)
+ *     field     = ifft2(spectrum)
+ * with H(z) = exp(-2*pi*i * kz * z), kz = sqrt(k0^2 - kx^2 - ky^2), k0 = 1/wl,
+ * kx = fftfreq(N, area_size/N).  The phase kz*z is reduced mod 1 cycle with
+ * ~48-bit (float-float) arithmetic, then exp() is taken in FP32.  Evanescent
+ * points pass through (H = 1) as in the reference, unless EVANESCENT_MASK.
+ * z == 0 is allowed here (H = 1); Beam2D.propagate(0) returns before calling.
+ * kmask is optional (LP_MASK_NONE): Beam2D.spectral_filter (beam2d.py:366-373)
+ * is this call with z = 0. */
+lp_status lp_propagate(lp_cfloat* spectrum, lp_cfloat* field, int n,
+                       double area_size, double wl, double z,
+                       const void* kmask, int kmask_type, uint32_t flags,
+                       void* stream);
+
+/* Fused field -> field step, one pass over HBM in and one out:
+ *     u        = field_in * L(lens_f) * xmask          (x domain)
+ *     S        = fft2(u) * kmask * H(z)                 (k domain, in registers)
+ *     field_out= ifft2(S)        [optional: spectrum_out = S, iprofile = |field_out|^2]
+ * It is Beam2D.lens(f) (beam2d.py:508-511) + coordinate_filter(f_init)
+ * (:339-342) + spectral_filter(f_init) (:370-373) + propagate(z) (:484-490)
+ * in one launch sequence with no intermediate field or H array in HBM.
+ * lens_f == 0 means no lens.  field_in == field_out is allowed.  Any of
+ * spectrum_out / iprofile_out may be NULL.  With LP_FLAG_ADJOINT the call
+ * applies the adjoint operator (conj masks, conj lens, H(-z)). */
+lp_status lp_propagate_field(const lp_cfloat* field_in, lp_cfloat* field_out,
+                             lp_cfloat* spectrum_out, float* iprofile_out,
+                             int n, double area_size, double wl, double z,
+                             double lens_f, const void* xmask, int xmask_type,
+                             const void* kmask, int kmask_type, uint32_t flags,
+                             void* stream);
+
+/* ------------------------------------------------------------- operators -- */
+/* Beam2D.lens(f) (beam2d.py:508-511): field *= exp(i*(X^2+Y^2)*k0/(2f));
+ * spectrum_out = fft2(field) (NULL: skip the transform). */
+lp_status lp_lens(lp_cfloat* field, lp_cfloat* spectrum_out, int n,
+                  double area_size, double wl, double f, void* stream);
+
+/* Beam2D.coordinate_filter(f_init=mask) (beam2d.py:339-342):
+ * field *= mask; spectrum_out = fft2(field) (NULL: skip the transform). */
+lp_status lp_coordinate_filter(lp_cfloat* field, lp_cfloat* spectrum_out,
+                               int n, const void* mask, int mask_type,
+                               void* stream);
+
+/* Beam2D.spectral_filter(f_init=mask) (beam2d.py:370-373):
+ * spectrum *= mask; field_out = ifft2(spectrum). */
+lp_status lp_spectral_filter(lp_cfloat* spectrum, lp_cfloat* field_out, int n,
+                             const void* mask, int mask_type, void* stream);
+
+/* Beam2D.iprofile (beam2d.py:717): out = |field|^2 as float32. */
+lp_status lp_iprofile(const lp_cfloat* field, float* out, int n, void* stream);
+
+/* spectrum *= H(z) only (no transform): used to materialise a spectrum whose
+ * propagation distance the caller kept pending. */
+lp_status lp_apply_transfer(lp_cfloat* spectrum, int n, double area_size,
+                            double wl, double z, uint32_t flags, void* stream);
+
+/* -------------------------------------------------- unfused comparison --
+ * The plain FFT -> multiply -> IFFT form on the same GPU, with H materialised
+ * in HBM by its own kernel, like the reference's numpy/CuPy sequence
+ * (beam2d.py:485-490).  LP_FLAG_PLAIN_FP64_H builds H from a float64 Kz grid
+ * in FP64 exactly like the reference; otherwise H uses the same float-float
+ * phase as the fused path. */
+#define LP_FLAG_PLAIN_FP64_H 0x100u
+lp_status lp_plain_propagate_field(const lp_cfloat* field_in,
+                                   lp_cfloat* field_out, int n,
+                                   double area_size, double wl, double z,
+                                   uint32_t flags, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LIGHTPROP2D_GB300_H */

@@ -1,0 +1,110 @@
+"""ctypes binding of the C ABI declared in ``include/lightprop2d_gb300.h``.
+
+The shared library is built in-tree by ``lightprop2d_gb300.build``.  There is
+no fallback: if the library is missing or a call fails, an exception says why.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblightprop2d_gb300.so")
+
+# lp_status codes (include/lightprop2d_gb300.h)
+LP_OK = 0
+LP_ERR_INVALID_ARGUMENT = 1
+LP_ERR_UNSUPPORTED_SIZE = 2
+LP_ERR_MISALIGNED = 3
+LP_ERR_CUDA = 4
+LP_ERR_OUT_OF_MEMORY = 5
+LP_ERR_NOT_INITIALIZED = 6
+LP_ERR_TIMEOUT = 7
+
+# mask element types
+LP_MASK_NONE = 0
+LP_MASK_F32 = 1
+LP_MASK_C64 = 2
+LP_MASK_U8 = 3
+LP_MASK_PHASE_F32 = 4
+LP_MASK_F64 = 5
+LP_MASK_C128 = 6
+
+# flags
+LP_FLAG_PHASE_FP32 = 0x1
+LP_FLAG_EVANESCENT_MASK = 0x2
+LP_FLAG_ADJOINT = 0x4
+LP_FLAG_SPECTRUM_READONLY = 0x8
+LP_FLAG_DZ = 0x10
+LP_FLAG_PLAIN_FP64_H = 0x100
+
+_vp, _i, _d, _u = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_uint32
+
+# name -> argtypes (restype is lp_status = int unless listed in _RESTYPES)
+SIGNATURES = {
+    "lp_abi_version": [],
+    "lp_last_error": [],
+    "lp_status_string": [_i],
+    "lp_is_supported_n": [_i],
+    "lp_init": [_i],
+    "lp_workspace_release": [],
+    "lp_profile_events": [ctypes.POINTER(ctypes.c_void_p), _i],
+    "lp_fft2": [_vp, _vp, _i, _i, _vp],
+    "lp_propagate": [_vp, _vp, _i, _d, _d, _d, _vp, _i, _u, _vp],
+    "lp_propagate_field": [_vp, _vp, _vp, _vp, _i, _d, _d, _d, _d, _vp, _i, _vp, _i,
+                           _u, _vp],
+    "lp_lens": [_vp, _vp, _i, _d, _d, _d, _vp],
+    "lp_coordinate_filter": [_vp, _vp, _i, _vp, _i, _vp],
+    "lp_spectral_filter": [_vp, _vp, _i, _vp, _i, _vp],
+    "lp_iprofile": [_vp, _vp, _i, _vp],
+    "lp_apply_transfer": [_vp, _i, _d, _d, _d, _u, _vp],
+    "lp_plain_propagate_field": [_vp, _vp, _i, _d, _d, _d, _u, _vp],
+}
+_RESTYPES = {"lp_last_error": ctypes.c_char_p, "lp_status_string": ctypes.c_char_p}
+
+_lib = None
+_lock = threading.Lock()
+
+
+class BackendError(RuntimeError):
+    """A CUDA-side failure reported by the backend."""
+
+
+def load():
+    """Load the shared library (once) and declare every ABI signature."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"{LIB_PATH} is missing: build it with "
+                "`python -c 'import lightprop2d_gb300.build as b; b.build()'` "
+                "(the GB300 backend has no CPU fallback)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, argtypes in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = argtypes
+            fn.restype = _RESTYPES.get(name, ctypes.c_int)
+        _lib = L
+        return _lib
+
+
+def last_error() -> str:
+    return load().lp_last_error().decode(errors="replace")
+
+
+def check(status: int, what: str) -> None:
+    """Raise the exception that matches an lp_status (reference-style errors:
+    ValueError for bad arguments, RuntimeError for device failures)."""
+    if status == LP_OK:
+        return
+    msg = f"{what}: {load().lp_status_string(status).decode()}: {last_error()}"
+    if status in (LP_ERR_INVALID_ARGUMENT, LP_ERR_UNSUPPORTED_SIZE, LP_ERR_MISALIGNED):
+        raise ValueError(msg)
+    if status == LP_ERR_OUT_OF_MEMORY:
+        raise MemoryError(msg)
+    raise BackendError(msg)

@@ -1,0 +1,368 @@
+"""``Beam2D`` with the API of lightprop2d/beam2d.py, backed by GB300 CUDA kernels.
+
+Same dataclass fields, methods and results as the reference class
+(beam2d.py:44-757) for the propagation path: the constructor, ``propagate``,
+``lens``, ``coordinate_filter``, ``spectral_filter``, ``field``,
+``spectrum``, ``iprofile``, ``phiprofile`` and the grid attributes
+``X, Y, Kx, Ky, Kz, k0, dL``.
+
+How the state is kept (observable results are the reference's):
+
+* ``field`` is a ``torch.complex64`` CUDA tensor.  Each operation that
+  replaces the field allocates a new tensor, as the reference rebinds
+  ``self.field``.
+* The spectrum is state (beam2d.py:489).  It is stored as a base grid plus a
+  pending propagation distance ``dz``: ``spectrum = base * H(dz)``.  So a
+  run of ``propagate`` calls reads the base spectrum and writes the field
+  (one inverse 2-D FFT per call, ``H`` made in registers), and the spectrum
+  is only multiplied out when someone reads ``beam.spectrum``.
+* After ``lens`` / ``coordinate_filter`` the reference recomputes
+  ``spectrum = fft2(field)``.  Here the x-domain multiplier is kept pending
+  and folded into the next transform, so ``lens(f); propagate(z)`` is one
+  fused field -> field pass sequence (lens in the first pass, H between the
+  forward and inverse column transforms).
+* Grids ``X, Y, Kx, Ky`` are host numpy arrays like the reference's CPU
+  path, so generator callables (``init_field_gen``, ``f_gen``) receive the
+  same arguments as in the reference; their results are uploaded once.
+
+Differences, by design:
+
+* Storage is complex64 whatever ``complex_bits`` says (the kernels compute
+  in complex64 with FP64-grade transfer phases; results agree with the
+  reference's complex128 path to ~1e-6 relative L2).  ``complex_bits=128``
+  issues one warning.
+* ``use_gpu`` is accepted for signature compatibility; the backend always
+  runs on a CUDA device.  ``numpy_output`` works as in the reference.
+* Supported ``npoints``: powers of two from 16 to 4096 (ValueError otherwise).
+"""
+from __future__ import annotations
+
+import math
+import warnings
+from collections.abc import Iterable
+from dataclasses import dataclass
+from typing import Callable, Union
+
+import numpy as np
+import torch
+
+from . import backend as B
+
+nm = 1e-7
+um = 1e-4
+mm = 1e-1
+cm = 1
+m = 100
+
+_warned_c128 = False
+
+
+def _to_device(a, device, dtype=torch.complex64) -> torch.Tensor:
+    if isinstance(a, torch.Tensor):
+        t = a.to(device=device)
+    elif isinstance(a, np.ndarray) or np.isscalar(a):
+        t = torch.as_tensor(np.ascontiguousarray(a), device=device)
+    else:
+        raise ValueError("Unknown type of the given array, not numpy array or torch tensor")
+    if dtype is not None and t.dtype != dtype:
+        t = t.to(dtype)
+    return t.contiguous()
+
+
+@dataclass
+class Beam2D:
+    """Electromagnetic field propagation using the spectral (angular-spectrum) method.
+
+    Parameters are those of lightprop2d.Beam2D (beam2d.py:79-91), lengths in cm.
+    """
+
+    area_size: float
+    npoints: int
+    wl: float
+    z: float = 0.
+    xp: object = torch
+    init_field: object = None
+    init_spectrum: object = None
+    init_field_gen: object = None
+    init_gen_args: tuple = ()
+    complex_bits: int = 128
+
+    use_gpu: bool = False
+    numpy_output: bool = True
+    device: object = None
+
+    # ------------------------------------------------------------ set-up --
+    def __post_init__(self):
+        global _warned_c128
+        self.xp = torch
+        if self.device is None:
+            self.device = torch.device("cuda", torch.cuda.current_device())
+        self.device = torch.device(self.device)
+        if self.device.type != "cuda":
+            raise ValueError("the GB300 backend needs a CUDA device")
+        if not B.is_supported(self.npoints):
+            raise ValueError(
+                f"npoints={self.npoints} is not supported by the GB300 backend "
+                "(powers of two from 16 to 4096)")
+        if self.complex_bits == 128 and not _warned_c128:
+            _warned_c128 = True
+            warnings.warn("complex_bits=128: the GB300 backend stores complex64 fields "
+                          "(transfer phases are evaluated to FP64-grade accuracy)")
+        self.complex = torch.complex64
+        B.init(self.device)
+        self._construct_grids()
+        if self.init_field_gen is not None:
+            f = self.init_field_gen(self.X, self.Y, *self.init_gen_args)
+        elif self.init_field is not None:
+            f = self.init_field
+        else:
+            raise ValueError(
+                "Init field data is None : " +
+                "'init_field_gen' must be a function or 'init_field' must be an array.")
+        self._field = _to_device(f, self.device)
+        self._check_grid(self._field, "init field")
+        self._pend_invf = 0.0   # pending lens: sum of 1/f
+        self._pend_xmask = None  # pending coordinate mask (device tensor)
+        if self.init_spectrum is None:
+            self._spec = None    # derived: fft2(field)
+        else:
+            self._spec = _to_device(self.init_spectrum, self.device)
+            self._check_grid(self._spec, "init spectrum")
+        self._spec_dz = 0.0
+
+    def _check_grid(self, t, what):
+        if tuple(t.shape) != (self.npoints, self.npoints):
+            raise ValueError(f"{what} must be {self.npoints}x{self.npoints}, "
+                             f"got {tuple(t.shape)}")
+
+    def _construct_grids(self):
+        """Grids as in beam2d.py:299-308; Kz is computed lazily on access."""
+        self.dL = self.area_size / self.npoints
+        self.X = np.arange(-self.npoints // 2, self.npoints // 2, 1) * self.dL
+        self.Y = self.X.reshape((-1, 1))
+        self.k0 = 1 / self.wl
+        self.Kx = np.fft.fftfreq(self.npoints, d=self.dL)
+        self.Ky = self.Kx.reshape((-1, 1))
+        self._Kz = None
+
+    @property
+    def Kz(self):
+        if self._Kz is None:
+            with np.errstate(invalid="ignore"):
+                self._Kz = np.nan_to_num(np.sqrt(self.k0 ** 2 - self.Kx ** 2 - self.Ky ** 2))
+        return self._Kz
+
+    # -------------------------------------------------------------- state --
+    def _has_pending(self) -> bool:
+        return self._pend_invf != 0.0 or self._pend_xmask is not None
+
+    def _flush_x(self):
+        """Apply pending x-domain multipliers to the field (new tensor)."""
+        if not self._has_pending():
+            return
+        f = self._field.clone()
+        if self._pend_invf != 0.0:
+            B.lens(f, self.area_size, self.wl, 1.0 / self._pend_invf)
+        if self._pend_xmask is not None:
+            B.coordinate_filter(f, self._pend_xmask)
+        self._field = f
+        self._pend_invf = 0.0
+        self._pend_xmask = None
+
+    @property
+    def field(self) -> torch.Tensor:
+        self._flush_x()
+        return self._field
+
+    @field.setter
+    def field(self, value):
+        # The reference keeps the spectrum when the field is assigned directly.
+        if self._spec is None:
+            self._materialise_spectrum()
+        self._pend_invf = 0.0
+        self._pend_xmask = None
+        self._field = _to_device(value, self.device)
+        self._check_grid(self._field, "field")
+
+    def _materialise_spectrum(self):
+        if self._spec is None:
+            self._flush_x()
+            self._spec = B.fft2(self._field)
+            self._spec_dz = 0.0
+        elif self._spec_dz != 0.0:
+            s = self._spec.clone()
+            B.apply_transfer(s, self.area_size, self.wl, self._spec_dz)
+            self._spec = s
+            self._spec_dz = 0.0
+
+    @property
+    def spectrum(self) -> torch.Tensor:
+        self._materialise_spectrum()
+        return self._spec
+
+    @spectrum.setter
+    def spectrum(self, value):
+        self._spec = _to_device(value, self.device)
+        self._check_grid(self._spec, "spectrum")
+        self._spec_dz = 0.0
+
+    # ---------------------------------------------------------- operators --
+    def _update_obj(self, field, spectrum=None):
+        """beam2d.py:231-288: reset z and swap in a new field (and spectrum)."""
+        self.z = 0
+        self._pend_invf = 0.0
+        self._pend_xmask = None
+        self._field = _to_device(field, self.device)
+        self._spec = None if spectrum is None else _to_device(spectrum, self.device)
+        self._spec_dz = 0.0
+
+    def propagate(self, z: float):
+        """Propagate by ``z`` cm (beam2d.py:462-490).
+
+        spectrum *= exp(-2*pi*i*Kz*z); field = ifft2(spectrum).
+        """
+        if z == 0:
+            return
+        self.z += z
+        if self._spec is not None:
+            # Spectrum is state: read base spectrum, apply H(dz_total) in
+            # registers, write only the field.
+            self._spec_dz += z
+            self._field = B.propagate(self._spec, self.area_size, self.wl, self._spec_dz,
+                                      write_spectrum=False)
+            return
+        # Spectrum derived from the field (+ pending lens/mask): one fused
+        # field -> field sequence that also stores the propagated spectrum.
+        spec = torch.empty_like(self._field)
+        lens_f = (1.0 / self._pend_invf) if self._pend_invf != 0.0 else 0.0
+        self._field = B.propagate_field(self._field, self.area_size, self.wl, z,
+                                        spectrum_out=spec, lens_f=lens_f,
+                                        xmask=self._pend_xmask)
+        self._pend_invf = 0.0
+        self._pend_xmask = None
+        self._spec = spec
+        self._spec_dz = 0.0
+
+    def lens(self, f: float):
+        """Thin lens exp(i*(X^2+Y^2)*k0/(2f)) (beam2d.py:492-511)."""
+        if not (isinstance(f, (int, float, np.floating)) and math.isfinite(f) and f != 0):
+            raise ValueError("focal length must be a finite non-zero number")
+        self._pend_invf += 1.0 / f
+        self._spec = None
+        self._spec_dz = 0.0
+
+    def _mask(self, f_init, f_gen, fargs, grid_x, grid_y):
+        m = None
+        if f_gen is not None:
+            assert callable(f_gen)
+            assert isinstance(fargs, Iterable)
+            m = _to_device(f_gen(grid_x, grid_y, *fargs), self.device, dtype=None)
+        if f_init is not None:
+            assert isinstance(f_init, (np.ndarray, torch.Tensor))
+            fi = _to_device(f_init, self.device, dtype=None)
+            m = fi if m is None else m * fi
+        if m is not None and m.dtype == torch.bool:
+            m = m.to(torch.uint8)
+        return m
+
+    def coordinate_filter(self, f_init=None, f_gen: Union[Callable, None] = None,
+                          fargs: tuple = ()) -> None:
+        """field *= f_gen(X, Y, *fargs) * f_init; spectrum = fft2(field)
+        (beam2d.py:310-342)."""
+        m = self._mask(f_init, f_gen, fargs, self.X, self.Y)
+        if m is None:
+            self._flush_x()
+            self._spec = None
+            return
+        if self._pend_xmask is not None:
+            self._flush_x()
+        self._pend_xmask = m
+        self._spec = None
+        self._spec_dz = 0.0
+
+    def spectral_filter(self, f_init=None, f_gen: Union[Callable, None] = None,
+                        fargs: tuple = ()) -> None:
+        """spectrum *= f_gen(Kx, Ky, *fargs) * f_init; field = ifft2(spectrum)
+        (beam2d.py:344-373)."""
+        m = self._mask(f_init, f_gen, fargs, self.Kx, self.Ky)
+        if self._spec is None:
+            spec = torch.empty_like(self._field)
+            lens_f = (1.0 / self._pend_invf) if self._pend_invf != 0.0 else 0.0
+            self._field = B.propagate_field(self._field, self.area_size, self.wl, 0.0,
+                                            spectrum_out=spec, lens_f=lens_f,
+                                            xmask=self._pend_xmask, kmask=m)
+            self._pend_invf = 0.0
+            self._pend_xmask = None
+            self._spec = spec
+        else:
+            spec = self._spec.clone()
+            self._field = B.propagate(spec, self.area_size, self.wl, self._spec_dz, kmask=m)
+            self._spec = spec
+        self._spec_dz = 0.0
+
+    # ----------------------------------------------------------- readouts --
+    def _np(self, t):
+        return t.cpu().numpy() if self.numpy_output else t
+
+    @property
+    def iprofile(self):
+        """|field|^2 (beam2d.py:706-721); numpy when numpy_output."""
+        return self._np(B.iprofile(self.field))
+
+    @property
+    def phiprofile(self):
+        """angle(field) (beam2d.py:723-738); numpy when numpy_output."""
+        return self._np(torch.angle(self.field))
+
+    @property
+    def centroid(self):
+        """Intensity-weighted centre (Xc, Yc, nxc, nyc) (beam2d.py:669-685)."""
+        n = self.npoints // 2
+        I = B.iprofile(self.field).double()
+        c = (torch.arange(-n, n, device=self.device, dtype=torch.float64) * self.dL)
+        tot = I.sum()
+        Xc = float((I.sum(0) * c).sum() / tot)
+        Yc = float((I.sum(1) * c).sum() / tot)
+        return Xc, Yc, int(Xc / self.dL) + n, int(Yc / self.dL) + n
+
+    @property
+    def D4sigma(self):
+        """Beam widths 4*sigma along x and y (beam2d.py:687-704)."""
+        n = self.npoints // 2
+        I = B.iprofile(self.field).double()
+        c = (torch.arange(-n, n, device=self.device, dtype=torch.float64) * self.dL)
+        Xc, Yc, _, _ = self.centroid
+        tot = I.sum()
+        sx = math.sqrt(float((I.sum(0) * (c - Xc) ** 2).sum() / tot))
+        sy = math.sqrt(float((I.sum(1) * (c - Yc) ** 2).sum() / tot))
+        return 4 * sx, 4 * sy
+
+    @property
+    def centroid_intensity(self) -> float:
+        """Intensity at the centroid pixel (beam2d.py:740-752)."""
+        _, _, nxc, nyc = self.centroid
+        return float(B.iprofile(self.field)[nyc, nxc])
+
+    # ---------------------------------------------- outside this backend --
+    def expand(self, area_size: float):
+        raise NotImplementedError("Beam2D.expand is not provided by the GB300 propagation backend")
+
+    def crop(self, area_size: float, npoints: int = 0):
+        raise NotImplementedError("Beam2D.crop is not provided by the GB300 propagation backend")
+
+    def coarse(self, mean_order: int = 1):
+        raise NotImplementedError("Beam2D.coarse is not provided by the GB300 propagation backend")
+
+    def lens_image(self, f: float, l1: float, l2: float):
+        raise NotImplementedError("Beam2D.lens_image is not provided by the GB300 propagation backend")
+
+    def deconstruct_by_modes(self, *a, **k):
+        raise NotImplementedError("mode decomposition is not provided by the GB300 propagation backend")
+
+    fast_deconstruct_by_modes = deconstruct_by_modes
+    construct_by_modes = deconstruct_by_modes
+
+    def __repr__(self) -> str:
+        return (f"Beam {self.npoints:d}x{self.npoints:d} points" +
+                f"\n\t{self.area_size:.3g}x{self.area_size:.3g} cm " +
+                f"\n\t<wl={self.wl / nm:.3g} nm, z={self.z:.3g} cm>")

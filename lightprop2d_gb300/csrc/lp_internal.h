@@ -1,0 +1,65 @@
+// Host-side interfaces shared by the translation units of the backend.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lp_device.cuh"
+
+namespace lp {
+
+// Work folded into a row (x-direction) pass.
+struct RowOps {
+  // Prologue, applied to the loaded field before the forward row transform.
+  int lens;                  // 1: multiply by exp(+-2*pi*i * kappa*(jx^2+jy^2))
+  float kap_hi, kap_lo;      // kappa = dL^2 * k0 / (4*pi*f) in cycles, float-float
+  const void* xmask;         // optional x-domain multiplier
+  int xmask_type;
+  int conj;                  // adjoint: conjugate every multiplier
+  // Epilogue, applied after the inverse row transform.
+  float scale;               // real factor on the output (1 = none)
+  float* iprofile;           // optional |out|^2 (float32)
+  const void* ymask;         // optional x-domain multiplier on the output
+  int ymask_type;
+};
+
+// Work folded into a column (y-direction) pass at the spectral point.
+struct ColOps {
+  KParams kp;
+  int apply_h;               // multiply by the transfer function
+  int phase_fp32;            // plain-FP32 phase variant
+  int evan_mask;             // H = 0 on evanescent points (reference: H = 1)
+  int conj;                  // adjoint: conjugate multipliers
+  int dz;                    // also multiply by -2*pi*i*k0*sqrt(v)  (d/dz)
+  const void* kmask;         // optional k-domain multiplier
+  int kmask_type;
+  float2* spectrum_out;      // optional write of the multiplied spectrum (pre-scale)
+  float scale;               // real factor applied after the spectral multipliers
+};
+
+enum ColMode { COL_FWD = 0, COL_INV = 1, COL_FUSED = 2 };
+
+// Launchers for one transform size.
+struct SizeOps {
+  int n;
+  cudaError_t (*init)();  // per-device set-up (twiddle table, smem attributes)
+  cudaError_t (*row)(int inverse, const float2* in, float2* out, const RowOps& ops,
+                     cudaStream_t st);
+  cudaError_t (*col)(int mode, const float2* in, float2* out, const ColOps& ops,
+                     cudaStream_t st);
+};
+
+const SizeOps* size_ops(int n);
+
+inline RowOps row_ops_none() {
+  RowOps o{};
+  o.scale = 1.0f;
+  return o;
+}
+inline ColOps col_ops_none() {
+  ColOps o{};
+  o.scale = 1.0f;
+  return o;
+}
+
+}  // namespace lp

@@ -1,0 +1,197 @@
+"""CPU oracle for the angular-spectrum propagation path of lightprop2d 1.0.4.
+
+TEST INFRASTRUCTURE ONLY.  This module is the checker: the CUDA backend in
+``lightprop2d_gb300`` never imports it.  Only ``tests/``, ``__graft_entry__.smoke``
+and the CPU-baseline leg of ``bench.py`` may use it.
+
+It restates, in plain numpy (float64 / complex128 unless told otherwise), the
+reference's own algorithm so that every GPU result can be compared with it:
+
+* grids ............ lightprop2d/beam2d.py:299-308 (``_construct_grids``) and
+                     :189-205 (``_k_grid`` -> ``fftfreq``)
+* fft2 / ifft2 ..... lightprop2d/beam2d.py:207-229 (numpy convention: the inverse
+                     carries the 1/N^2 factor)
+* propagate ........ lightprop2d/beam2d.py:481-490
+* lens ............. lightprop2d/beam2d.py:508-511
+* coordinate_filter  lightprop2d/beam2d.py:335-342
+* spectral_filter .. lightprop2d/beam2d.py:366-373
+* iprofile ......... lightprop2d/beam2d.py:717-721
+
+Parity is pinned: ``tests/test_oracle.py`` checks this module against golden
+vectors produced by running the reference itself (``tests/golden/make_golden.py``).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+nm = 1e-7
+um = 1e-4
+mm = 1e-1
+cm = 1
+m = 100
+
+
+def grids(area_size: float, npoints: int, wl: float) -> dict:
+    """Grids exactly as ``Beam2D._construct_grids`` builds them (beam2d.py:299-308).
+
+    X is a centred row vector, Y its column; Kx = fftfreq(N, dL) is unshifted
+    and in cycles/cm; Kz = nan_to_num(sqrt(k0^2 - Kx^2 - Ky^2)) so evanescent
+    entries become 0 (a pass-through of the transfer function, not a mask).
+    """
+    dL = area_size / npoints
+    X = np.arange(-npoints // 2, npoints // 2, 1) * dL
+    Y = X.reshape((-1, 1))
+    k0 = 1 / wl
+    Kx = np.fft.fftfreq(npoints, d=dL)
+    Ky = Kx.reshape((-1, 1))
+    with np.errstate(invalid="ignore"):
+        Kz = np.nan_to_num(np.sqrt(k0 ** 2 - Kx ** 2 - Ky ** 2))
+    return dict(dL=dL, X=X, Y=Y, k0=k0, Kx=Kx, Ky=Ky, Kz=Kz)
+
+
+def fft2(a: np.ndarray) -> np.ndarray:
+    """beam2d.py:217 (numpy path): unnormalised forward 2-D DFT."""
+    return np.fft.fft2(a)
+
+
+def ifft2(a: np.ndarray) -> np.ndarray:
+    """beam2d.py:229 (numpy path): inverse 2-D DFT with the 1/N^2 factor."""
+    return np.fft.ifft2(a)
+
+
+def transfer(Kz: np.ndarray, z: float) -> np.ndarray:
+    """exp(i*phase) with phase = 2*pi*(trunc(Kz*z) - Kz*z), beam2d.py:485-489."""
+    dk = Kz * z
+    phase = 2 * np.pi * (np.trunc(dk) - dk)
+    return np.cos(phase) + 1j * np.sin(phase)
+
+
+def propagate(spectrum: np.ndarray, Kz: np.ndarray, z: float):
+    """``Beam2D.propagate`` body (beam2d.py:481-490).
+
+    Returns (spectrum_new, field_new).  ``z == 0`` is a no-op in the reference
+    (returns before touching anything); callers handle that case.  The in-place
+    ``*=`` of the reference casts the complex128 transfer function into the
+    spectrum's dtype, which ``np.multiply(..., out=)`` reproduces.
+    """
+    s = spectrum.copy()
+    np.multiply(s, transfer(Kz, z), out=s, casting="same_kind")
+    return s, ifft2(s)
+
+
+def lens_phase(X: np.ndarray, Y: np.ndarray, k0: float, f: float) -> np.ndarray:
+    """exp(i*(X^2+Y^2)*k0/(2f)) as built in beam2d.py:508-510 (k0 = 1/wl, no 2*pi)."""
+    phase = (X ** 2 + Y ** 2) * k0 / (2 * f)
+    return np.cos(phase) + 1j * np.sin(phase)
+
+
+def lens(field: np.ndarray, X, Y, k0: float, f: float):
+    """``Beam2D.lens`` body (beam2d.py:508-511): returns (field_new, spectrum_new)."""
+    fl = field.copy()
+    np.multiply(fl, lens_phase(X, Y, k0, f), out=fl, casting="same_kind")
+    return fl, fft2(fl)
+
+
+def coordinate_filter(field: np.ndarray, mask: np.ndarray):
+    """``Beam2D.coordinate_filter`` with an array mask (beam2d.py:339-342)."""
+    fl = field.copy()
+    np.multiply(fl, mask, out=fl, casting="same_kind")
+    return fl, fft2(fl)
+
+
+def spectral_filter(spectrum: np.ndarray, mask: np.ndarray):
+    """``Beam2D.spectral_filter`` with an array mask (beam2d.py:370-373)."""
+    s = spectrum.copy()
+    np.multiply(s, mask, out=s, casting="same_kind")
+    return s, ifft2(s)
+
+
+def iprofile(field: np.ndarray) -> np.ndarray:
+    """|field|^2 (beam2d.py:717)."""
+    return np.abs(field) ** 2
+
+
+class OracleBeam:
+    """Stateful restatement of ``Beam2D`` for the propagation path.
+
+    Holds (field, spectrum, z) like the reference dataclass (beam2d.py:79-133):
+    the spectrum is state, ``propagate`` multiplies it in place and overwrites
+    the field; ``lens`` / ``coordinate_filter`` overwrite the spectrum.
+    """
+
+    def __init__(self, area_size, npoints, wl, init_field=None,
+                 init_spectrum=None, complex_bits=128):
+        g = grids(area_size, npoints, wl)
+        self.area_size, self.npoints, self.wl = area_size, npoints, wl
+        self.__dict__.update(g)
+        self.complex = np.complex64 if complex_bits == 64 else np.complex128
+        if init_field is None:
+            raise ValueError("init_field is required")
+        self.field = np.asarray(init_field).astype(self.complex)
+        self.spectrum = (fft2(self.field) if init_spectrum is None
+                         else np.asarray(init_spectrum))
+        self.z = 0.0
+
+    def propagate(self, z):
+        if z == 0:
+            return
+        self.z += z
+        self.spectrum, self.field = propagate(self.spectrum, self.Kz, z)
+
+    def lens(self, f):
+        self.field, self.spectrum = lens(self.field, self.X, self.Y, self.k0, f)
+
+    def coordinate_filter(self, mask):
+        self.field, self.spectrum = coordinate_filter(self.field, mask)
+
+    def spectral_filter(self, mask):
+        self.spectrum, self.field = spectral_filter(self.spectrum, mask)
+
+    @property
+    def iprofile(self):
+        return iprofile(self.field)
+
+
+# --------------------------------------------------------------------------
+# Error metrics used by every parity test.
+# --------------------------------------------------------------------------
+
+def rel_l2(a, b) -> float:
+    """||a - b||_2 / ||b||_2 in float64 (b is the oracle)."""
+    a = np.asarray(a, dtype=np.complex128)
+    b = np.asarray(b, dtype=np.complex128)
+    nb = np.linalg.norm(b.ravel())
+    return float(np.linalg.norm((a - b).ravel()) / (nb if nb > 0 else 1.0))
+
+
+def energy_err(a, b) -> float:
+    """|sum|a|^2 - sum|b|^2| / sum|b|^2 (energy conservation vs the oracle)."""
+    ea = float(np.sum(np.abs(np.asarray(a, dtype=np.complex128)) ** 2))
+    eb = float(np.sum(np.abs(np.asarray(b, dtype=np.complex128)) ** 2))
+    return abs(ea - eb) / (eb if eb > 0 else 1.0)
+
+
+# --------------------------------------------------------------------------
+# Seeded input builders for the benchmark / parity workloads.  They compose
+# the reference's generators (profiles.py) the way each workload describes.
+# --------------------------------------------------------------------------
+
+def random_phase_hole(npoints, area_size, radius, seed):
+    """Round hole of geometric radius ``radius`` (r <= radius), amplitude
+    U[0,1) and phase 2*pi*U[0,1) from ``np.random.default_rng(seed)``, zero
+    outside.  Used for the 256^2 / 200 um / 632 nm CPU workload.
+    """
+    g = grids(area_size, npoints, 1.0)
+    rng = np.random.default_rng(seed)
+    amp = rng.uniform(size=(npoints, npoints))
+    ph = rng.uniform(size=(npoints, npoints))
+    r2 = g["X"] ** 2 + g["Y"] ** 2
+    f = amp * np.exp(2j * np.pi * ph)
+    f[r2 > radius ** 2] = 0
+    return f
+
+
+def gaussian(npoints, area_size, A0, rho0):
+    """profiles.gaussian_beam (profiles.py:64-71) on the Beam2D grid."""
+    g = grids(area_size, npoints, 1.0)
+    return A0 * np.exp(-(g["X"] ** 2 + g["Y"] ** 2) / rho0 ** 2)

@@ -1,0 +1,73 @@
+"""CPU: the C-ABI library loads and exports every symbol the header declares;
+argument checks that fail before any CUDA call behave as documented."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "lightprop2d_gb300.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from lightprop2d_gb300 import build
+    build.build()
+    from lightprop2d_gb300 import _lib
+    return _lib.load()
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(lp_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert "lp_propagate" in names and "lp_propagate_field" in names
+    assert len(names) >= 15
+
+
+def test_every_declared_symbol_is_exported(lib):
+    from lightprop2d_gb300 import _lib
+    for name in declared_functions():
+        assert hasattr(lib, name), f"{name} missing from the shared library"
+        assert name in _lib.SIGNATURES, f"{name} has no ctypes signature"
+
+
+def test_meta_calls(lib):
+    assert lib.lp_abi_version() == 1
+    for n in (16, 32, 64, 128, 256, 512, 1024, 2048, 4096):
+        assert lib.lp_is_supported_n(n) == 1
+    for n in (0, 8, 100, 8192, -4):
+        assert lib.lp_is_supported_n(n) == 0
+    assert lib.lp_status_string(0) == b"ok"
+
+
+def test_validation_before_any_device_call(lib):
+    from lightprop2d_gb300 import _lib as L
+    vp = ctypes.c_void_p
+    # unsupported size: rejected before touching CUDA
+    st = lib.lp_fft2(vp(256), vp(256), 100, 0, vp(0))
+    assert st == L.LP_ERR_UNSUPPORTED_SIZE
+    assert b"npoints=100" in lib.lp_last_error()
+    # NULL pointer
+    st = lib.lp_fft2(vp(0), vp(256), 64, 0, vp(0))
+    assert st == L.LP_ERR_INVALID_ARGUMENT
+    # misaligned pointer
+    st = lib.lp_fft2(vp(260), vp(256), 64, 0, vp(0))
+    assert st == L.LP_ERR_MISALIGNED
+    # bad geometry
+    st = lib.lp_propagate(vp(256), vp(512), 64, -1.0, 1e-4, 1.0, vp(0), 0, 0, vp(0))
+    assert st == L.LP_ERR_INVALID_ARGUMENT
+    # bad mask type
+    st = lib.lp_propagate(vp(256), vp(512), 64, 1.0, 1e-4, 1.0, vp(0), 99, 0, vp(0))
+    assert st == L.LP_ERR_INVALID_ARGUMENT
+    with pytest.raises(ValueError):
+        L.check(L.LP_ERR_UNSUPPORTED_SIZE, "x")
+    with pytest.raises(MemoryError):
+        L.check(L.LP_ERR_OUT_OF_MEMORY, "x")
+    with pytest.raises(L.BackendError):
+        L.check(L.LP_ERR_CUDA, "x")
