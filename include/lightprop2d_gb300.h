@@ -13,9 +13,11 @@
  *   - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
  *     asynchronous with respect to the host; results are ready once the
  *     stream reaches them.
- *   - Ownership: the caller owns every buffer passed in.  The library keeps
- *     per-device twiddle tables (static device arrays) and a per-(device,
- *     stream) scratch grid that lp_workspace_release() frees.
+ *   - Ownership: the caller owns every buffer passed in.  The transforms keep
+ *     their intermediates in the caller's output grid, so the fused paths
+ *     allocate nothing; the library keeps per-device twiddle tables (static
+ *     device arrays) and, for the unfused comparison path only, a
+ *     per-(device, stream) H grid that lp_workspace_release() frees.
  *   - Errors: every call returns an lp_status; no exception crosses the ABI.
  *     lp_last_error() returns a thread-local message for the last failure.
  *   - Supported N: powers of two from 16 to 4096.  Other N return
@@ -107,7 +109,7 @@ lp_status lp_fft2(const lp_cfloat* in, lp_cfloat* out, int n, int inverse,
  * points pass through (H = 1) as in the reference, unless EVANESCENT_MASK.
  * z == 0 is allowed here (H = 1); Beam2D.propagate(0) returns before calling.
  * kmask is optional (LP_MASK_NONE): Beam2D.spectral_filter (beam2d.py:366-373)
- * is this call with z = 0. */
+ * is this call with z = 0.  spectrum and field must be different grids. */
 lp_status lp_propagate(lp_cfloat* spectrum, lp_cfloat* field, int n,
                        double area_size, double wl, double z,
                        const void* kmask, int kmask_type, uint32_t flags,
@@ -120,9 +122,11 @@ lp_status lp_propagate(lp_cfloat* spectrum, lp_cfloat* field, int n,
  * It is Beam2D.lens(f) (beam2d.py:508-511) + coordinate_filter(f_init)
  * (:339-342) + spectral_filter(f_init) (:370-373) + propagate(z) (:484-490)
  * in one launch sequence with no intermediate field or H array in HBM.
- * lens_f == 0 means no lens.  field_in == field_out is allowed.  Any of
- * spectrum_out / iprofile_out may be NULL.  With LP_FLAG_ADJOINT the call
- * applies the adjoint operator (conj masks, conj lens, H(-z)). */
+ * lens_f == 0 means no lens.  field_in == field_out is allowed;
+ * spectrum_out must differ from field_out.  Any of spectrum_out /
+ * iprofile_out may be NULL.  With LP_FLAG_ADJOINT the call applies the
+ * adjoint operator: conj(kmask*H) in the k domain and conj(lens*xmask)
+ * applied after the inverse transform. */
 lp_status lp_propagate_field(const lp_cfloat* field_in, lp_cfloat* field_out,
                              lp_cfloat* spectrum_out, float* iprofile_out,
                              int n, double area_size, double wl, double z,

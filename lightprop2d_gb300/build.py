@@ -37,23 +37,26 @@ def sources() -> list[str]:
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
-def _fingerprint() -> str:
+def _fingerprint(extra_flags=()) -> str:
     h = hashlib.sha256()
     for d in (CSRC, os.path.join(ROOT, "include")):
         for f in sorted(os.listdir(d)):
             with open(os.path.join(d, f), "rb") as fh:
                 h.update(f.encode() + fh.read())
-    h.update(" ".join(ARCH + NVCC_FLAGS).encode())
+    h.update(" ".join(ARCH + NVCC_FLAGS + list(extra_flags)).encode())
     return h.hexdigest()
 
 
 def build(verbose: bool = False, force: bool = False, jobs: int | None = None,
           extra_flags: list[str] | None = None) -> str:
-    """Compile (if stale) and return the path of the shared library."""
-    fp = _fingerprint()
+    """Compile (if stale) and return the path of the shared library.
+
+    ``extra_flags`` (e.g. ``-DLP_MIN_BLOCKS=3``) select a tuning variant; the
+    stamp records them, so a later default build recompiles."""
+    fp = _fingerprint(extra_flags or ())
     stamp = os.path.join(BUILD, "stamp")
     if (not force and os.path.exists(LIB_PATH) and os.path.exists(stamp)
-            and open(stamp).read() == fp and not extra_flags):
+            and open(stamp).read() == fp):
         return LIB_PATH
     os.makedirs(BUILD, exist_ok=True)
     nvcc = _nvcc()

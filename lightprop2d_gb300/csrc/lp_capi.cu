@@ -108,10 +108,10 @@ lp_status ensure_ready(cudaStream_t st, int* dev_out) {
   return init_device(dev);
 }
 
-// Scratch grids cached per (device, stream).
+// Scratch grids of the unfused comparison path, cached per (device, stream).
+// The fused paths need none: each pass reads whole lines into registers
+// before writing them back, so intermediates live in the output grid.
 struct Scratch {
-  void* tmp = nullptr;
-  size_t tmp_bytes = 0;
   void* hbuf = nullptr;
   size_t hbuf_bytes = 0;
   void* kz = nullptr;
@@ -142,14 +142,6 @@ lp_status grow(void** p, size_t* have, size_t need, const char* what) {
 
 Scratch& scratch_for(int dev, cudaStream_t st) {
   return g_scratch[std::make_pair(dev, (uintptr_t)st)];
-}
-
-lp_status get_tmp(int dev, cudaStream_t st, size_t bytes, float2** out) {
-  std::lock_guard<std::mutex> lk(g_mu);
-  Scratch& s = scratch_for(dev, st);
-  lp_status r = grow(&s.tmp, &s.tmp_bytes, bytes, "transpose scratch");
-  *out = reinterpret_cast<float2*>(s.tmp);
-  return r;
 }
 
 // ---------------------------------------------------------------- checks --
@@ -329,11 +321,12 @@ int ew_grid(size_t n2) {
   return (int)(g > 152 * 16 ? 152 * 16 : (g ? g : 1));
 }
 
-// Forward 2-D transform: rows (with x-domain prologue ops) then columns.
-lp_status run_fft2_fwd(const SizeOps* so, const float2* in, float2* out, float2* tmp,
-                       const RowOps& rops, cudaStream_t st) {
-  LP_CUDA(so->row(0, in, tmp, rops, st), "row pass (forward)");
-  LP_CUDA(so->col(COL_FWD, tmp, out, col_ops_none(), st), "column pass (forward)");
+// Forward 2-D transform: rows (with x-domain prologue ops) then columns, the
+// intermediate kept in `out`.
+lp_status run_fft2_fwd(const SizeOps* so, const float2* in, float2* out, const RowOps& rops,
+                       cudaStream_t st) {
+  LP_CUDA(so->row(0, in, out, rops, st), "row pass (forward)");
+  LP_CUDA(so->col(COL_FWD, out, out, col_ops_none(), st), "column pass (forward)");
   return LP_OK;
 }
 
@@ -378,7 +371,7 @@ lp_status lp_workspace_release(void) {
   for (auto& kv : g_scratch) {
     cudaSetDevice(kv.first.first);
     Scratch& s = kv.second;
-    for (void* p : {s.tmp, s.hbuf, s.kz})
+    for (void* p : {s.hbuf, s.kz})
       if (p && cudaFree(p) != cudaSuccess) r = fail(LP_ERR_CUDA, "cudaFree failed");
   }
   g_scratch.clear();
@@ -402,15 +395,13 @@ lp_status lp_fft2(const lp_cfloat* in, lp_cfloat* out, int n, int inverse, void*
   int dev;
   LP_TRY(ensure_ready(st, &dev));
   const SizeOps* so = size_ops(n);
-  float2* tmp;
-  LP_TRY(get_tmp(dev, st, sizeof(float2) * n * n, &tmp));
   const float2* src = reinterpret_cast<const float2*>(in);
   float2* dst = reinterpret_cast<float2*>(out);
-  if (!inverse) return run_fft2_fwd(so, src, dst, tmp, row_ops_none(), st);
+  if (!inverse) return run_fft2_fwd(so, src, dst, row_ops_none(), st);
   ColOps c = col_ops_none();
   c.scale = 1.0f / ((float)n * (float)n);
-  LP_CUDA(so->col(COL_INV, src, tmp, c, st), "column pass (inverse)");
-  LP_CUDA(so->row(1, tmp, dst, row_ops_none(), st), "row pass (inverse)");
+  LP_CUDA(so->col(COL_INV, src, dst, c, st), "column pass (inverse)");
+  LP_CUDA(so->row(1, dst, dst, row_ops_none(), st), "row pass (inverse)");
   return LP_OK;
 }
 
@@ -423,23 +414,23 @@ lp_status lp_propagate(lp_cfloat* spectrum, lp_cfloat* field, int n, double area
   LP_TRY(check_mask(kmask, kmask_type, "kmask"));
   LP_TRY(check_geometry(area_size, wl));
   if (!std::isfinite(z)) return fail(LP_ERR_INVALID_ARGUMENT, "z must be finite");
+  if ((const void*)spectrum == (const void*)field)
+    return fail(LP_ERR_INVALID_ARGUMENT, "spectrum and field must be different grids");
   cudaStream_t st = (cudaStream_t)stream;
   int dev;
   LP_TRY(ensure_ready(st, &dev));
   const SizeOps* so = size_ops(n);
-  float2* tmp;
-  LP_TRY(get_tmp(dev, st, sizeof(float2) * n * n, &tmp));
+  float2* f = reinterpret_cast<float2*>(field);
   ColOps c = make_colops(n, area_size, wl, z, z != 0.0 || (flags & LP_FLAG_DZ), flags);
   c.kmask = kmask_type ? kmask : nullptr;
   c.kmask_type = kmask_type;
   if (!(flags & LP_FLAG_SPECTRUM_READONLY)) c.spectrum_out = reinterpret_cast<float2*>(spectrum);
   c.scale = 1.0f / ((float)n * (float)n);
   mark(0, st);
-  LP_CUDA(so->col(COL_INV, reinterpret_cast<const float2*>(spectrum), tmp, c, st),
+  LP_CUDA(so->col(COL_INV, reinterpret_cast<const float2*>(spectrum), f, c, st),
           "column pass (transfer + inverse)");
   mark(1, st);
-  LP_CUDA(so->row(1, tmp, reinterpret_cast<float2*>(field), row_ops_none(), st),
-          "row pass (inverse)");
+  LP_CUDA(so->row(1, f, f, row_ops_none(), st), "row pass (inverse)");
   mark(2, st);
   return LP_OK;
 }
@@ -460,33 +451,43 @@ lp_status lp_propagate_field(const lp_cfloat* field_in, lp_cfloat* field_out,
   LP_TRY(check_geometry(area_size, wl));
   if (!std::isfinite(z) || !std::isfinite(lens_f))
     return fail(LP_ERR_INVALID_ARGUMENT, "z and lens_f must be finite");
+  if (spectrum_out && (const void*)spectrum_out == (const void*)field_out)
+    return fail(LP_ERR_INVALID_ARGUMENT, "spectrum_out and field_out must be different grids");
   cudaStream_t st = (cudaStream_t)stream;
   int dev;
   LP_TRY(ensure_ready(st, &dev));
   const SizeOps* so = size_ops(n);
-  float2* tmp;
-  LP_TRY(get_tmp(dev, st, sizeof(float2) * n * n, &tmp));
+  float2* out = reinterpret_cast<float2*>(field_out);
 
-  RowOps r = row_ops_none();
-  if (lens_f != 0.0) set_lens(r, n, area_size, wl, lens_f);
-  r.xmask = xmask_type ? xmask : nullptr;
-  r.xmask_type = xmask_type;
-  r.conj = (flags & LP_FLAG_ADJOINT) ? 1 : 0;
+  // x-domain multiplier: before the forward transform, or -- for the adjoint
+  // operator diag(conj(L*m)) F^-1 diag(conj(kmask*H)) F -- after the inverse.
+  const bool adjoint = (flags & LP_FLAG_ADJOINT) != 0;
+  RowOps x = row_ops_none();
+  if (lens_f != 0.0) set_lens(x, n, area_size, wl, lens_f);
+  x.xmask = xmask_type ? xmask : nullptr;
+  x.xmask_type = xmask_type;
+  x.conj = adjoint ? 1 : 0;
+  RowOps r = row_ops_none(), e = row_ops_none();
+  if (adjoint) {
+    e = x;
+    e.x_at_store = 1;
+  } else {
+    r = x;
+  }
+  e.iprofile = iprofile_out;
   ColOps c = make_colops(n, area_size, wl, z, z != 0.0 || (flags & LP_FLAG_DZ), flags);
   c.kmask = kmask_type ? kmask : nullptr;
   c.kmask_type = kmask_type;
   c.spectrum_out = reinterpret_cast<float2*>(spectrum_out);
   c.scale = 1.0f / ((float)n * (float)n);
-  RowOps e = row_ops_none();
-  e.iprofile = iprofile_out;
 
   mark(0, st);
-  LP_CUDA(so->row(0, reinterpret_cast<const float2*>(field_in), tmp, r, st),
+  LP_CUDA(so->row(0, reinterpret_cast<const float2*>(field_in), out, r, st),
           "row pass (forward)");
   mark(1, st);
-  LP_CUDA(so->col(COL_FUSED, tmp, tmp, c, st), "column pass (forward, transfer, inverse)");
+  LP_CUDA(so->col(COL_FUSED, out, out, c, st), "column pass (forward, transfer, inverse)");
   mark(2, st);
-  LP_CUDA(so->row(1, tmp, reinterpret_cast<float2*>(field_out), e, st), "row pass (inverse)");
+  LP_CUDA(so->row(1, out, out, e, st), "row pass (inverse)");
   mark(3, st);
   return LP_OK;
 }
@@ -501,10 +502,8 @@ static lp_status xdomain_op(lp_cfloat* field, lp_cfloat* spectrum_out, int n, Ro
   xmul_kernel<<<ew_grid(n2), 256, 0, st>>>(f, n, r);
   LP_CUDA(cudaGetLastError(), "x-domain multiply");
   if (!spectrum_out) return LP_OK;
-  float2* tmp;
-  LP_TRY(get_tmp(dev, st, sizeof(float2) * n2, &tmp));
-  return run_fft2_fwd(size_ops(n), f, reinterpret_cast<float2*>(spectrum_out), tmp,
-                      row_ops_none(), st);
+  return run_fft2_fwd(size_ops(n), f, reinterpret_cast<float2*>(spectrum_out), row_ops_none(),
+                      st);
 }
 
 lp_status lp_lens(lp_cfloat* field, lp_cfloat* spectrum_out, int n, double area_size,
@@ -584,8 +583,7 @@ lp_status lp_plain_propagate_field(const lp_cfloat* field_in, lp_cfloat* field_o
   LP_TRY(ensure_ready(st, &dev));
   const SizeOps* so = size_ops(n);
   const size_t n2 = (size_t)n * n;
-  float2* tmp;
-  LP_TRY(get_tmp(dev, st, sizeof(float2) * n2, &tmp));
+  float2* out = reinterpret_cast<float2*>(field_out);
   float2* h;
   double* kz = nullptr;
   bool build_kz = false;
@@ -612,19 +610,18 @@ lp_status lp_plain_propagate_field(const lp_cfloat* field_in, lp_cfloat* field_o
     build_kz_fp64_kernel<<<g, 256, 0, st>>>(kz, n, 1.0 / (n * dL), 1.0 / wl);
     LP_CUDA(cudaGetLastError(), "Kz build");
   }
-  LP_TRY(run_fft2_fwd(so, reinterpret_cast<const float2*>(field_in), tmp, tmp, row_ops_none(), st));
+  LP_TRY(run_fft2_fwd(so, reinterpret_cast<const float2*>(field_in), out, row_ops_none(), st));
   if (kz)
     build_h_fp64_kernel<<<g, 256, 0, st>>>(h, kz, n2, z);
   else
     build_h_kernel<<<g, 256, 0, st>>>(h, n, make_colops(n, area_size, wl, z, true, flags));
   LP_CUDA(cudaGetLastError(), "H build");
-  cmul_inplace_kernel<<<g, 256, 0, st>>>(tmp, h, n2);
+  cmul_inplace_kernel<<<g, 256, 0, st>>>(out, h, n2);
   LP_CUDA(cudaGetLastError(), "spectrum *= H");
   ColOps c = col_ops_none();
   c.scale = 1.0f / ((float)n * (float)n);
-  LP_CUDA(so->col(COL_INV, tmp, tmp, c, st), "column pass (inverse)");
-  LP_CUDA(so->row(1, tmp, reinterpret_cast<float2*>(field_out), row_ops_none(), st),
-          "row pass (inverse)");
+  LP_CUDA(so->col(COL_INV, out, out, c, st), "column pass (inverse)");
+  LP_CUDA(so->row(1, out, out, row_ops_none(), st), "row pass (inverse)");
   return LP_OK;
 }
 

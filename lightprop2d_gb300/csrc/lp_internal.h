@@ -10,17 +10,19 @@ namespace lp {
 
 // Work folded into a row (x-direction) pass.
 struct RowOps {
-  // Prologue, applied to the loaded field before the forward row transform.
+  // x-domain multiplier: lens phase and/or mask, applied to the loaded line
+  // before the transform, or (x_at_store) to the transformed line before it
+  // is stored -- the adjoint of "multiply, then transform" is "transform,
+  // then multiply by the conjugate".
   int lens;                  // 1: multiply by exp(+-2*pi*i * kappa*(jx^2+jy^2))
   float kap_hi, kap_lo;      // kappa = dL^2 * k0 / (4*pi*f) in cycles, float-float
   const void* xmask;         // optional x-domain multiplier
   int xmask_type;
-  int conj;                  // adjoint: conjugate every multiplier
-  // Epilogue, applied after the inverse row transform.
+  int conj;                  // conjugate the multiplier
+  int x_at_store;            // apply after the transform instead of before
+  // Epilogue.
   float scale;               // real factor on the output (1 = none)
   float* iprofile;           // optional |out|^2 (float32)
-  const void* ymask;         // optional x-domain multiplier on the output
-  int ymask_type;
 };
 
 // Work folded into a column (y-direction) pass at the spectral point.
