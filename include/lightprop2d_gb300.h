@@ -171,6 +171,23 @@ lp_status lp_plain_propagate_field(const lp_cfloat* field_in,
                                    double area_size, double wl, double z,
                                    uint32_t flags, void* stream);
 
+/* No counterpart in the reference.  The same unfused propagate as
+ * lp_plain_propagate_field (float-float H; flags must be 0) for callers that
+ * cannot call cudaMalloc while running -- a host application that reserved
+ * nearly all device memory for its own pool, or a real-time loop that forbids
+ * device allocation after start-up because cudaMalloc can block the device.
+ * Its H grid lives in a fixed device array of 1024 x 1024 complex64 (8 MiB),
+ * held by every device that loads the library until exit, so it allocates
+ * nothing.  N above 1024 returns LP_ERR_UNSUPPORTED_SIZE.  All calls on a
+ * device share that array: calls that overlap on the GPU race (serialise
+ * them).  The first call on a device does its one-time set-up; make it
+ * before any stream capture. */
+lp_status lp_plain_propagate_field_noalloc(const lp_cfloat* field_in,
+                                           lp_cfloat* field_out, int n,
+                                           double area_size, double wl,
+                                           double z, uint32_t flags,
+                                           void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -60,6 +60,7 @@ SIGNATURES = {
     "lp_iprofile": [_vp, _vp, _i, _vp],
     "lp_apply_transfer": [_vp, _i, _d, _d, _d, _u, _vp],
     "lp_plain_propagate_field": [_vp, _vp, _i, _d, _d, _d, _u, _vp],
+    "lp_plain_propagate_field_noalloc": [_vp, _vp, _i, _d, _d, _d, _u, _vp],
 }
 _RESTYPES = {"lp_last_error": ctypes.c_char_p, "lp_status_string": ctypes.c_char_p}
 

@@ -332,6 +332,11 @@ lp_status run_fft2_fwd(const SizeOps* so, const float2* in, float2* out, const R
 
 }  // namespace
 
+int lp::set_last_error(int s, const char* msg) {
+  t_last_error = msg;
+  return s;
+}
+
 // =================================================================== ABI ==
 extern "C" {
 

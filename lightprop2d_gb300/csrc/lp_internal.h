@@ -53,6 +53,9 @@ struct SizeOps {
 
 const SizeOps* size_ops(int n);
 
+// Sets the thread-local text returned by lp_last_error() and returns `s`.
+int set_last_error(int s, const char* msg);
+
 inline RowOps row_ops_none() {
   RowOps o{};
   o.scale = 1.0f;
