@@ -91,6 +91,12 @@ lp_status lp_workspace_release(void);
  * events[i] after pass i (3 passes for lp_propagate_field, 2 for
  * lp_propagate).  Thread-local. */
 lp_status lp_profile_events(void** events, int count);
+/* Tuning hook (no counterpart in the reference): resident CTAs per SM for the
+ * persistent row (kind 0) or column (kind 1) kernels of size n; value 0
+ * restores the built-in choice (the count whose last wave is fullest).
+ * Returns the count now in effect, or -1 for a bad n / kind.  Process-wide;
+ * set by the autotuner (lightprop2d_gb300.tune), not needed otherwise. */
+int lp_tune_ctas_per_sm(int n, int kind, int value);
 
 /* ------------------------------------------------------------ transforms --
  * numpy convention: forward unnormalised, inverse scaled by 1/N^2.

@@ -11,7 +11,7 @@
 #include <string>
 #include <utility>
 
-#include "../../include/lightprop2d_gb300.h"
+#include "lightprop2d_gb300.h"
 #include "lp_internal.h"
 
 namespace lp {
@@ -359,6 +359,12 @@ const char* lp_status_string(int s) {
 }
 
 int lp_is_supported_n(int n) { return size_ops(n) ? 1 : 0; }
+
+int lp_tune_ctas_per_sm(int n, int kind, int value) {
+  const SizeOps* so = size_ops(n);
+  if (!so || (kind != 0 && kind != 1)) return -1;
+  return so->set_ctas_per_sm(kind, value);
+}
 
 lp_status lp_init(int device) {
   int count = 0;

@@ -49,6 +49,9 @@ struct SizeOps {
                      cudaStream_t st);
   cudaError_t (*col)(int mode, const float2* in, float2* out, const ColOps& ops,
                      cudaStream_t st);
+  // Resident CTAs per SM for the persistent row (kind 0) / column (kind 1)
+  // kernels; 0 restores the built-in choice.  Returns the value in effect.
+  int (*set_ctas_per_sm)(int kind, int value);
 };
 
 const SizeOps* size_ops(int n);

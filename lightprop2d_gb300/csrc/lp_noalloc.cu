@@ -28,7 +28,7 @@
 #include <cstdio>
 #include <mutex>
 
-#include "../../include/lightprop2d_gb300.h"
+#include "lightprop2d_gb300.h"
 #include "lp_internal.h"
 
 using namespace lp;
