@@ -71,6 +71,8 @@ typedef enum lp_mask_type {
 #define LP_FLAG_ADJOINT 0x4u            /* conjugate every multiplier: the adjoint operator */
 #define LP_FLAG_SPECTRUM_READONLY 0x8u  /* lp_propagate: do not write spectrum*H back */
 #define LP_FLAG_DZ 0x10u                /* multiply the spectrum by -2*pi*i*kz as well (d/dz) */
+#define LP_FLAG_XMASK_AFTER 0x20u       /* lp_propagate_field: apply lens/xmask after the
+                                           inverse transform (propagate, then screen) */
 
 /* ---------------------------------------------------------------- meta -- */
 int lp_abi_version(void);
@@ -130,9 +132,11 @@ lp_status lp_propagate(lp_cfloat* spectrum, lp_cfloat* field, int n,
  * in one launch sequence with no intermediate field or H array in HBM.
  * lens_f == 0 means no lens.  field_in == field_out is allowed;
  * spectrum_out must differ from field_out.  Any of spectrum_out /
- * iprofile_out may be NULL.  With LP_FLAG_ADJOINT the call applies the
- * adjoint operator: conj(kmask*H) in the k domain and conj(lens*xmask)
- * applied after the inverse transform. */
+ * iprofile_out may be NULL.  LP_FLAG_XMASK_AFTER moves the x-domain
+ * multiplier after the inverse transform (field_out = m * P(field_in)).
+ * With LP_FLAG_ADJOINT the call applies the adjoint operator: conj(kmask*H)
+ * in the k domain and conj(lens*xmask) on the opposite side of the
+ * transforms. */
 lp_status lp_propagate_field(const lp_cfloat* field_in, lp_cfloat* field_out,
                              lp_cfloat* spectrum_out, float* iprofile_out,
                              int n, double area_size, double wl, double z,

@@ -37,6 +37,7 @@ LP_FLAG_EVANESCENT_MASK = 0x2
 LP_FLAG_ADJOINT = 0x4
 LP_FLAG_SPECTRUM_READONLY = 0x8
 LP_FLAG_DZ = 0x10
+LP_FLAG_XMASK_AFTER = 0x20
 LP_FLAG_PLAIN_FP64_H = 0x100
 
 _vp, _i, _d, _u = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_uint32

@@ -470,16 +470,18 @@ lp_status lp_propagate_field(const lp_cfloat* field_in, lp_cfloat* field_out,
   const SizeOps* so = size_ops(n);
   float2* out = reinterpret_cast<float2*>(field_out);
 
-  // x-domain multiplier: before the forward transform, or -- for the adjoint
-  // operator diag(conj(L*m)) F^-1 diag(conj(kmask*H)) F -- after the inverse.
+  // x-domain multiplier m: before the forward transform (P(m u)) or, with
+  // XMASK_AFTER, after the inverse (m P(u)).  The adjoint conjugates every
+  // multiplier and moves m to the other side: (P diag(m))^H = diag(conj(m)) P^H.
   const bool adjoint = (flags & LP_FLAG_ADJOINT) != 0;
+  const bool after = ((flags & LP_FLAG_XMASK_AFTER) != 0) != adjoint;
   RowOps x = row_ops_none();
   if (lens_f != 0.0) set_lens(x, n, area_size, wl, lens_f);
   x.xmask = xmask_type ? xmask : nullptr;
   x.xmask_type = xmask_type;
   x.conj = adjoint ? 1 : 0;
   RowOps r = row_ops_none(), e = row_ops_none();
-  if (adjoint) {
+  if (after) {
     e = x;
     e.x_at_store = 1;
   } else {
