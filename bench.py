@@ -102,6 +102,141 @@ def run_reference(args):
     return 0
 
 
+# ------------------------------------------------------------ batch workload --
+# 4096 beams: 64% 256^2, 25% 512^2, 9% 1024^2, 2% 2048^2 (1,171,062,784 points).
+BATCH_MIX = ((256, 2621), (512, 1024), (1024, 369), (2048, 82))
+BATCH_WL = 632e-7
+
+
+def batch_workload(dev, seed=3, mix=BATCH_MIX):
+    """Seeded uneven-size batch, generated on the device: per beam a round
+    hole of radius U[0.05, 0.40]*A (amplitude U[0,1), phase U[0,2pi)), area
+    A = U[200 um, 2 mm], lens f = U[1, 20] cm, z = U[0.5, 20] cm, wl 632 nm.
+    Beams of one size are slices of one (count, n, n) tensor.  Returns a dict
+    of per-beam lists (fields, iprofiles, area, z, f, n)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    out = {k: [] for k in ("fields", "iprofiles", "area", "z", "f", "n")}
+    out["stacks"] = []
+    for n, cnt in mix:
+        frac = rng.uniform(0.05, 0.40, cnt)
+        out["area"] += list(rng.uniform(200e-4, 0.2, cnt))
+        out["f"] += list(rng.uniform(1.0, 20.0, cnt))
+        out["z"] += list(rng.uniform(0.5, 20.0, cnt))
+        st = torch.empty(cnt, n, n, dtype=torch.complex64, device=dev)
+        ip = torch.empty(cnt, n, n, dtype=torch.float32, device=dev)
+        j = torch.arange(-n // 2, n // 2, device=dev, dtype=torch.float64)
+        r2 = j[None, :] ** 2 + j[:, None] ** 2          # (x^2 + y^2) / dL^2
+        chunk = max(1, (1 << 25) // (n * n))
+        for c0 in range(0, cnt, chunk):
+            c1 = min(cnt, c0 + chunk)
+            amp = torch.rand(c1 - c0, n, n, generator=gen, device=dev)
+            ph = torch.rand(c1 - c0, n, n, generator=gen, device=dev) * (2 * np.pi)
+            thr = torch.as_tensor((frac[c0:c1] * n) ** 2, device=dev)  # (radius/dL)^2
+            amp = amp * (r2[None] <= thr[:, None, None])
+            st[c0:c1] = torch.polar(amp, ph)
+        out["stacks"].append((st, ip))
+        out["fields"] += [st[i] for i in range(cnt)]
+        out["iprofiles"] += [ip[i] for i in range(cnt)]
+        out["n"] += [n] * cnt
+    return out
+
+
+def batch_section(dev, stream, clocks, reps, check_oracle=True):
+    """Config: the uneven batch as one persistent launch in a CUDA graph
+    (autotuned options), against the same beams as per-beam fused calls."""
+    import torch
+    from lightprop2d_gb300 import _lib as L
+    from lightprop2d_gb300 import backend as B
+    from lightprop2d_gb300 import tune
+    from lightprop2d_gb300.batch import BeamBatch
+    from oracle import lp_oracle as O
+
+    W = batch_workload(dev)
+    nb, pts = len(W["fields"]), sum(n * n for n in W["n"])
+    # parity sample: first beam of every size, kept on the host before any run
+    pick = [W["n"].index(n) for n, _ in BATCH_MIX]
+    keep = {i: W["fields"][i].cpu().numpy() for i in pick}
+    args = (W["area"], BATCH_WL, W["z"], W["f"], W["iprofiles"])
+    bb = BeamBatch(W["fields"], *args)
+    bb.run()
+    bb.status()
+    torch.cuda.synchronize()
+    errs = {}
+    if check_oracle:
+        for i in pick:
+            n = W["n"][i]
+            g = O.grids(W["area"][i], n, BATCH_WL)
+            x, _ = O.lens(keep[i].astype(np.complex128), g["X"], g["Y"], g["k0"], W["f"][i])
+            _, x = O.propagate(O.fft2(x), g["Kz"], W["z"][i])
+            errs[str(n)] = O.rel_l2(W["fields"][i].cpu().numpy(), x)
+    bb.close()
+    del keep
+
+    with clocks.window():
+        best, table = tune.autotune_batch(W["fields"], *args, reps=3)
+    bb = BeamBatch(W["fields"], *args, **best)
+    info = bb.info()
+    graph = bb.capture()
+
+    def ev_time(fn, k):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(k):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / k
+
+    with clocks.window():
+        t_graph = ev_time(graph.replay, reps)
+    bb.status()
+
+    # the same beams as one fused field->field call each (3 launches per beam)
+    fl, ipl = W["fields"], W["iprofiles"]
+
+    def per_beam():
+        for i in range(nb):
+            B.propagate_field(fl[i], W["area"][i], BATCH_WL, W["z"][i], out=fl[i],
+                              iprofile_out=ipl[i], lens_f=W["f"][i])
+
+    with clocks.window():
+        t_calls = ev_time(per_beam, max(2, reps // 4))
+        g2 = torch.cuda.CUDAGraph()
+        s2 = torch.cuda.Stream(device=dev)
+        s2.wait_stream(stream)
+        with torch.cuda.stream(s2):
+            with torch.cuda.graph(g2, stream=s2):
+                per_beam()
+        stream.wait_stream(s2)
+        t_calls_graph = ev_time(g2.replay, max(2, reps // 2))
+    bb.close()
+    del graph, g2
+    alg = 20 * pts  # field read + write, iprofile write
+    return {
+        "workload": "4096 beams: " + ", ".join(f"{c} x {n}^2" for n, c in BATCH_MIX)
+                    + f" ({pts} points), hole+lens+propagate+iprofile, wl 632 nm",
+        "beams_per_s": round(nb / (t_graph * 1e-3), 1),
+        "points_per_s": round(pts / (t_graph * 1e-3), 1),
+        "ms_per_batch": round(t_graph, 4),
+        "effective_gbs": round(alg / (t_graph * 1e-3) / 1e9, 1),
+        "alg_bytes_per_batch": alg,
+        "launches_per_batch": 1,
+        "plan": {**best, **info},
+        "autotune_ms": {str(k): round(v, 4) for k, v in table.items()},
+        "per_beam_calls_ms": round(t_calls, 4),
+        "per_beam_calls_graph_ms": round(t_calls_graph, 4),
+        "speedup_vs_per_beam_graph": round(t_calls_graph / t_graph, 3),
+        "rel_l2_vs_fp64_oracle": errs,
+        "l2": f"{pts * 8 / 2**30:.1f} GiB of fields per batch (> L2)",
+    }
+
+
 # ----------------------------------------------------------------- GPU side --
 class ClockSampler:
     """nvidia-smi sampling of SM clocks and throttle reasons."""

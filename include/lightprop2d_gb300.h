@@ -169,6 +169,51 @@ lp_status lp_iprofile(const lp_cfloat* field, float* out, int n, void* stream);
 lp_status lp_apply_transfer(lp_cfloat* spectrum, int n, double area_size,
                             double wl, double z, uint32_t flags, void* stream);
 
+/* ------------------------------------------------------------- batches --
+ * Many beams of uneven grid sizes in ONE persistent launch.  Each beam runs
+ * lens(lens_f) -> propagate(z) -> iprofile on its own grid, in place:
+ *     field = ifft2( fft2(field * L) * H(z) ),  iprofile = |field|^2
+ * (Beam2D.lens + Beam2D.propagate + Beam2D.iprofile per beam; no reference
+ * counterpart for the batching itself).  Work items (beam, pass, tiles) are
+ * pulled from a device queue by resident CTAs; a column pass waits, with a
+ * bounded spin, on its beam's row pass (and so on).  Supported n: 64..4096.
+ * lp_batch_run is one kernel launch that allocates nothing, so it can be
+ * captured in a CUDA graph; the device counters reset themselves at the end of
+ * every run. */
+typedef struct lp_beam_desc {
+  lp_cfloat* field;  /* n x n complex64, input and output (in place) */
+  float* iprofile;   /* optional n x n float32 output |field|^2, or NULL */
+  int n;
+  double area_size, wl, z;
+  double lens_f;     /* 0: no lens */
+  uint32_t flags;    /* LP_FLAG_PHASE_FP32 | LP_FLAG_EVANESCENT_MASK */
+} lp_beam_desc;
+
+typedef struct lp_batch_options {
+  int ctas_per_sm;          /* resident CTAs per SM; 0: as many as fit */
+  int tiles_per_item;       /* tiles (4096 points each) per queue item; 0: 8 */
+  int group_points_log2;    /* beams are scheduled in groups of ~2^k points; 0: 23 */
+  long long spin_limit;     /* wait iterations (~200 ns each) before LP_ERR_TIMEOUT; 0: 2^22 */
+  int debug_unsatisfiable;  /* test hook: one dependency that is never met, so the run
+                               ends through the timeout path; 0 otherwise */
+} lp_batch_options;
+
+typedef struct lp_batch lp_batch;
+
+/* Plans a batch: sorts beams (largest first), builds the work queue and
+ * copies it to the device (this call allocates device memory). */
+lp_status lp_batch_create(const lp_beam_desc* beams, int count,
+                          const lp_batch_options* options, lp_batch** out);
+/* One persistent launch over the whole batch on `stream`. */
+lp_status lp_batch_run(lp_batch* batch, void* stream);
+/* Synchronises `stream`, then reads and clears the batch's device error flag:
+ * LP_OK, or LP_ERR_TIMEOUT when a bounded wait gave up during the last run. */
+lp_status lp_batch_status(lp_batch* batch, void* stream);
+/* Queue and launch shape: items, CTAs launched, resident CTAs per SM. */
+lp_status lp_batch_info(const lp_batch* batch, int* n_items, int* grid,
+                        int* ctas_per_sm);
+lp_status lp_batch_destroy(lp_batch* batch);
+
 /* -------------------------------------------------- unfused comparison --
  * The plain FFT -> multiply -> IFFT form on the same GPU, with H materialised
  * in HBM by its own kernel, like the reference's numpy/CuPy sequence

@@ -42,6 +42,20 @@ LP_FLAG_PLAIN_FP64_H = 0x100
 
 _vp, _i, _d, _u = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_uint32
 
+
+class BeamDesc(ctypes.Structure):
+    """lp_beam_desc"""
+    _fields_ = [("field", ctypes.c_void_p), ("iprofile", ctypes.c_void_p), ("n", ctypes.c_int),
+                ("area_size", ctypes.c_double), ("wl", ctypes.c_double), ("z", ctypes.c_double),
+                ("lens_f", ctypes.c_double), ("flags", ctypes.c_uint32)]
+
+
+class BatchOptions(ctypes.Structure):
+    """lp_batch_options"""
+    _fields_ = [("ctas_per_sm", ctypes.c_int), ("tiles_per_item", ctypes.c_int),
+                ("group_points_log2", ctypes.c_int), ("spin_limit", ctypes.c_longlong),
+                ("debug_unsatisfiable", ctypes.c_int)]
+
 # name -> argtypes (restype is lp_status = int unless listed in _RESTYPES)
 SIGNATURES = {
     "lp_abi_version": [],
@@ -63,6 +77,12 @@ SIGNATURES = {
     "lp_apply_transfer": [_vp, _i, _d, _d, _d, _u, _vp],
     "lp_plain_propagate_field": [_vp, _vp, _i, _d, _d, _d, _u, _vp],
     "lp_plain_propagate_field_noalloc": [_vp, _vp, _i, _d, _d, _d, _u, _vp],
+    "lp_batch_create": [ctypes.POINTER(BeamDesc), _i, ctypes.POINTER(BatchOptions),
+                        ctypes.POINTER(ctypes.c_void_p)],
+    "lp_batch_run": [_vp, _vp],
+    "lp_batch_status": [_vp, _vp],
+    "lp_batch_info": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)],
+    "lp_batch_destroy": [_vp],
 }
 _RESTYPES = {"lp_last_error": ctypes.c_char_p, "lp_status_string": ctypes.c_char_p}
 

@@ -86,6 +86,13 @@ lp_status init_device(int dev) {
       return cuda_fail(e, "per-size set-up");
     }
   }
+  {
+    cudaError_t e = batch_init();
+    if (e != cudaSuccess) {
+      if (prev != dev) cudaSetDevice(prev);
+      return cuda_fail(e, "batch kernel set-up");
+    }
+  }
   if (prev != dev) LP_CUDA(cudaSetDevice(prev), "cudaSetDevice");
   g_ready[dev] = true;
   return LP_OK;
@@ -185,8 +192,10 @@ lp_status check_geometry(double area, double wl) {
     if (s_ != LP_OK) return s_;    \
   } while (0)
 
+}  // namespace
+
 // Transfer-function constants (see lp_device.cuh: kz_phase_ff).
-KParams make_kparams(int n, double area, double wl, double z) {
+KParams lp::make_kparams(int n, double area, double wl, double z) {
   const double dL = area / n;               // beam2d.py:299
   const double val = 1.0 / (n * dL);        // numpy fftfreq spacing (beam2d.py:205)
   const double k0 = 1.0 / wl;               // beam2d.py:304
@@ -202,7 +211,7 @@ KParams make_kparams(int n, double area, double wl, double z) {
   return kp;
 }
 
-ColOps make_colops(int n, double area, double wl, double z, bool apply_h, uint32_t flags) {
+ColOps lp::make_colops(int n, double area, double wl, double z, bool apply_h, uint32_t flags) {
   ColOps o = col_ops_none();
   o.kp = make_kparams(n, area, wl, z);
   o.apply_h = apply_h ? 1 : 0;
@@ -213,7 +222,7 @@ ColOps make_colops(int n, double area, double wl, double z, bool apply_h, uint32
   return o;
 }
 
-void set_lens(RowOps& o, int n, double area, double wl, double f) {
+void lp::set_lens(RowOps& o, int n, double area, double wl, double f) {
   // (X^2+Y^2)*k0/(2f) radians with X = jx*dL  ->  kappa*(jx^2+jy^2) cycles.
   const double dL = area / n;
   const double kap = dL * dL * (1.0 / wl) / (4.0 * kPi * f);
@@ -222,6 +231,8 @@ void set_lens(RowOps& o, int n, double area, double wl, double f) {
   o.kap_hi = k.hi;
   o.kap_lo = k.lo;
 }
+
+namespace {
 
 // ------------------------------------------------------ elementwise kernels --
 __global__ void iprofile_kernel(const float2* __restrict__ f, float* __restrict__ out, size_t n2) {

@@ -270,9 +270,13 @@ __device__ __forceinline__ float kz_phase_ff(const KParams& kp, float a_hi, floa
   float u_hi, u_lo;
   two_prod(kp.beta_hi, qy, u_hi, u_lo);
   u_lo = fmaf(kp.beta_lo, qy, u_lo);
-  float v_hi, e;
-  two_sum(a_hi, -u_hi, v_hi, e);
-  const float v_lo = e + (a_lo - u_lo);
+  float v0, e, v_hi, v_lo;
+  two_sum(a_hi, -u_hi, v0, e);
+  // Renormalise: near the evanescent cut-off v0 is tiny after cancellation
+  // and the low part can exceed ulp(v0); the one-step Newton square root
+  // below needs |v_lo| <= ulp(v_hi) or its quadratic error reaches 1e-4
+  // cycles there.
+  two_sum(v0, e + (a_lo - u_lo), v_hi, v_lo);
   evanescent = !(v_hi > 0.0f);
   const float vv = evanescent ? 1.0f : v_hi;
   const float y = rsqrtf(vv);

@@ -1,0 +1,373 @@
+// 2-D FFT building blocks for any grid size N (templated; usable from any
+// translation unit): the per-line transform, the x-domain and spectral
+// multipliers, and "tiles" -- L rows or C columns of one N x N grid processed
+// by one CTA -- which the per-size pass kernels and the batched persistent
+// kernel are made of.
+//
+// A 1-D transform of length N runs on T = N/16 threads that each keep 16
+// points in registers.  Thread t holds the elements {t + T*j : j < 16} of its
+// line both before and after the transform (natural order), so a forward
+// transform, a pointwise spectral multiply and an inverse transform chain
+// with no reordering.
+//
+// The transform is a mixed-radix Stockham sequence (radix 16, then 16, then
+// 16/8/4/2 as N needs).  Stage s with radix R and Ns = product of the
+// earlier radices computes, for each butterfly b < N/R,
+//     a[r] = x[b + r*N/R] * W_(Ns*R)^(r*(b mod Ns))      (r < R)
+//     y[(b/Ns)*Ns*R + (b mod Ns) + r*Ns] = DFT_R(a)[r],
+// thread t doing butterflies b = t + q*T (q < 16/R).  Between stages the
+// line goes through one padded shared-memory buffer (element i at
+// i + i/16, which keeps the stride-16 writes of the first stage free of bank
+// conflicts).  Every stage is one small register butterfly, so the kernels
+// stay small enough for the SM instruction cache; per-point multipliers are
+// evaluated in rolled loops for the same reason.
+#pragma once
+
+#include <cmath>
+
+#include "lp_device.cuh"
+#include "lp_internal.h"
+
+namespace lp {
+
+template <int N>
+struct Plan;  // radices of the stages (0 = no stage)
+template <> struct Plan<16> { static constexpr int R[3] = {16, 0, 0}; };
+template <> struct Plan<32> { static constexpr int R[3] = {16, 2, 0}; };
+template <> struct Plan<64> { static constexpr int R[3] = {16, 4, 0}; };
+template <> struct Plan<128> { static constexpr int R[3] = {16, 8, 0}; };
+template <> struct Plan<256> { static constexpr int R[3] = {16, 16, 0}; };
+template <> struct Plan<512> { static constexpr int R[3] = {16, 16, 2}; };
+template <> struct Plan<1024> { static constexpr int R[3] = {16, 16, 4}; };
+template <> struct Plan<2048> { static constexpr int R[3] = {16, 16, 8}; };
+template <> struct Plan<4096> { static constexpr int R[3] = {16, 16, 16}; };
+
+constexpr int cmin(int a, int b) { return a < b ? a : b; }
+constexpr int cmax(int a, int b) { return a > b ? a : b; }
+
+template <int N>
+struct FftGeo {
+  static constexpr int T = N / 16;  // threads per line
+  static constexpr int NST = Plan<N>::R[2] ? 3 : Plan<N>::R[1] ? 2 : 1;
+  static constexpr int BUF = N + N / 16;  // padded line buffer (float2)
+  // Twiddle table offsets: stage 1 at 0 (R1*16 entries), stage 2 after it.
+  static constexpr int NS1 = 16, NS2 = 16 * Plan<N>::R[1];
+  static constexpr int TW_OFF1 = 0, TW_OFF2 = Plan<N>::R[1] * NS1;
+  static constexpr int TW_SIZE = TW_OFF2 + Plan<N>::R[2] * NS2 + 1;
+};
+
+// Host: the stage twiddles of size N, layout per stage [r][k] = W_(Ns*R)^(r*k)
+// (forward sign), computed in double and rounded once.
+template <int N>
+inline void fill_twiddles(float2* tw) {
+  using G = FftGeo<N>;
+  auto fill = [&](int off, int R, int NS) {
+    for (int r = 0; r < R; ++r)
+      for (int k = 0; k < NS; ++k) {
+        const double ang = -2.0 * kPi * (double)(r * k) / (double)(NS * R);
+        tw[off + r * NS + k] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+      }
+  };
+  if (G::NST >= 2) fill(G::TW_OFF1, Plan<N>::R[1], G::NS1);
+  if (G::NST >= 3) fill(G::TW_OFF2, Plan<N>::R[2], G::NS2);
+  tw[G::TW_SIZE - 1] = make_float2(1.0f, 0.0f);
+}
+
+__device__ __forceinline__ int pad16(int i) { return i + (i >> 4); }
+
+// Programmatic dependent launch: wait for the previous kernel's results, and
+// let the next kernel's CTAs be scheduled as this grid's CTAs retire.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;"); }
+
+// Shared-memory slot of line element i: interleaved (IL: lines fastest, for
+// column CTAs whose lanes run across lines) or one buffer per line (rows).
+template <int N, bool IL, int LINES>
+__device__ __forceinline__ int sidx(int i, int line) {
+  if constexpr (IL) return pad16(i) * LINES + line;
+  else return line * FftGeo<N>::BUF + pad16(i);
+}
+
+template <bool CTA>
+__device__ __forceinline__ void line_sync() {
+  if constexpr (CTA) __syncthreads(); else __syncwarp();
+}
+
+// Global loads / stores; CG = cache at L2 only (data produced by other CTAs
+// of the same launch must not be served from a stale L1 line).
+template <bool CG>
+__device__ __forceinline__ float2 gld(const float2* p) {
+  if constexpr (CG) return __ldcg(p); else return *p;
+}
+template <bool CG>
+__device__ __forceinline__ void gst(float2* p, float2 v) {
+  if constexpr (CG) __stcg(p, v); else *p = v;
+}
+
+// Stage 0 (radix 16, Ns = 1): element t + T*r of the input is v[r]; output r
+// goes to element t*16 + r of the buffer.  The buffer must be free.
+template <int N, int S, bool IL, int LINES>
+__device__ __forceinline__ void fft_first(float2 (&v)[16], float2* buf, int t, int line) {
+  Dft<16, S>::run(v);
+  if constexpr (FftGeo<N>::NST > 1) {
+    static_for<16>([&](auto rc) {
+      constexpr int r = decltype(rc)::value;
+      buf[sidx<N, IL, LINES>(t * 16 + r, line)] = v[r];
+    });
+  }
+}
+
+// Stage s > 0: inputs from shared memory, twiddled, DFT, outputs to shared
+// memory (middle stage) or to registers in natural order (last stage).
+template <int N, int S, int s, bool IL, int LINES, bool CTA>
+__device__ __forceinline__ void fft_stage(float2 (&v)[16], float2* buf, const float2* tw, int t,
+                                          int line) {
+  using G = FftGeo<N>;
+  constexpr int R = Plan<N>::R[s], T = G::T, nb = 16 / R;
+  constexpr int NS = (s == 1) ? G::NS1 : G::NS2;
+  constexpr int OFF = (s == 1) ? G::TW_OFF1 : G::TW_OFF2;
+  constexpr bool LAST = (s == G::NST - 1);
+  line_sync<CTA>();
+  static_for<nb>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    const int b = t + q * T;
+    static_for<R>([&](auto rc) {
+      constexpr int r = decltype(rc)::value;
+      v[q + nb * r] = buf[sidx<N, IL, LINES>(b + r * (N / R), line)];
+    });
+  });
+  if constexpr (!LAST) line_sync<CTA>();
+  static_for<nb>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    const int b = t + q * T;
+    const int k = b & (NS - 1);
+    float2 a[R];
+    static_for<R>([&](auto rc) { a[decltype(rc)::value] = v[q + nb * decltype(rc)::value]; });
+    static_for<R - 1>([&](auto rc) {
+      constexpr int r = decltype(rc)::value + 1;
+      float2 w = tw[OFF + r * NS + k];
+      if constexpr (S > 0) w.y = -w.y;
+      a[r] = cmul(a[r], w);
+    });
+    Dft<R, S>::run(a);
+    if constexpr (LAST) {
+      static_for<R>([&](auto rc) { v[q + nb * decltype(rc)::value] = a[decltype(rc)::value]; });
+    } else {
+      const int o = (b / NS) * NS * R + k;
+      static_for<R>([&](auto rc) {
+        constexpr int r = decltype(rc)::value;
+        buf[sidx<N, IL, LINES>(o + r * NS, line)] = a[r];
+      });
+    }
+  });
+}
+
+// Stages after the first (natural-order result in registers).  tw: the
+// stage twiddles of size N (shared memory).
+template <int N, int S, bool IL, int LINES, bool CTA>
+__device__ __forceinline__ void fft_rest(float2 (&v)[16], float2* buf, const float2* tw, int t,
+                                         int line) {
+  if constexpr (FftGeo<N>::NST >= 2) fft_stage<N, S, 1, IL, LINES, CTA>(v, buf, tw, t, line);
+  if constexpr (FftGeo<N>::NST == 3) fft_stage<N, S, 2, IL, LINES, CTA>(v, buf, tw, t, line);
+}
+
+__device__ __forceinline__ void conj16(float2 (&v)[16]) {
+  static_for<16>([&](auto jc) { v[decltype(jc)::value] = cconj(v[decltype(jc)::value]); });
+}
+
+// ------------------------------------------------------------------ rows --
+// x-domain multiplier (lens phase and/or mask) for row y at column x.
+template <int N>
+__device__ __forceinline__ float2 xop_value(int y, int x, const RowOps& ops) {
+  float2 m = make_float2(1.0f, 0.0f);
+  if (ops.lens) {
+    const float jx = (float)(x - N / 2), jy = (float)(y - N / 2);
+    m = cis_cycles(lens_cycles(ops.kap_hi, ops.kap_lo, fmaf(jx, jx, jy * jy)), 1.0f);
+  }
+  if (ops.xmask) m = cmul(m, mask_value(ops.xmask, ops.xmask_type, (size_t)y * N + x));
+  if (ops.conj) m = cconj(m);
+  return m;
+}
+
+// Multiply the thread's 16 points of row y by the x-domain multiplier,
+// evaluated in a rolled loop into the thread's own buffer slots (one copy of
+// the phase code), then applied.  The slots must be free.
+template <int N>
+__device__ __forceinline__ void apply_xops(float2 (&v)[16], float2* slots, int nthreads, int y,
+                                           int t, const RowOps& ops) {
+  constexpr int T = FftGeo<N>::T;
+  const int tid = threadIdx.x;
+#pragma unroll 1
+  for (int j = 0; j < 16; ++j) slots[j * nthreads + tid] = xop_value<N>(y, t + T * j, ops);
+  static_for<16>([&](auto jc) {
+    constexpr int j = decltype(jc)::value;
+    v[j] = cmul(v[j], slots[j * nthreads + tid]);
+  });
+}
+
+template <int N, bool CG = false>
+__device__ __forceinline__ void load_row(float2 (&v)[16], const float2* in, int y, int t) {
+  constexpr int T = FftGeo<N>::T;
+  const float2* src = in + (size_t)y * N + t;
+  static_for<16>([&](auto jc) { v[decltype(jc)::value] = gld<CG>(src + T * decltype(jc)::value); });
+}
+
+// Row tile: rows tile*L .. tile*L+L-1 by the CTA's first L*T threads, thread
+// (line g = threadIdx.x / T, t = threadIdx.x % T).  v holds the thread's
+// loaded points of row tile*L + g; `after_first` runs after the first stage
+// (the per-size kernels prefetch the next tile there).  The exchange buffer
+// (L * BUF floats2) must be free on entry.
+template <int N, int S, int L, int NT, bool CG, class Hook>
+__device__ __forceinline__ void row_tile(float2 (&v)[16], float2* out, int tile, const RowOps& ops,
+                                         float2* buf, const float2* tw, Hook after_first) {
+  constexpr int T = FftGeo<N>::T;
+  constexpr bool CTA = T > 32;
+  const int g = threadIdx.x / T, t = threadIdx.x % T;
+  const int y = tile * L + g;
+  const bool xops = ops.lens || ops.xmask;
+  if (xops && !ops.x_at_store) {
+    apply_xops<N>(v, buf, NT, y, t, ops);
+    __syncthreads();
+  }
+  fft_first<N, S, false, L>(v, buf, t, g);
+  after_first();
+  fft_rest<N, S, false, L, CTA>(v, buf, tw, t, g);
+  if (ops.scale != 1.0f) {
+    static_for<16>([&](auto jc) { v[decltype(jc)::value] = cscale(v[decltype(jc)::value], ops.scale); });
+  }
+  if (xops && ops.x_at_store) {
+    __syncthreads();
+    apply_xops<N>(v, buf, NT, y, t, ops);
+  }
+  float2* dst = out + (size_t)y * N + t;
+  static_for<16>([&](auto jc) { gst<CG>(dst + T * decltype(jc)::value, v[decltype(jc)::value]); });
+  if (ops.iprofile) {
+    float* ip = ops.iprofile + (size_t)y * N + t;
+    static_for<16>([&](auto jc) {
+      constexpr int j = decltype(jc)::value;
+      ip[T * j] = fmaf(v[j].x, v[j].x, v[j].y * v[j].y);
+    });
+  }
+}
+
+// --------------------------------------------------------------- columns --
+// Spectral multiplier without the mask at (|sy|, sx): H(z) [* d/dz factor].
+template <int N>
+__device__ __forceinline__ float2 transfer_value(int sy_abs, int sx, const ColOps& ops) {
+  const float qx = (float)(sx * sx), qy = (float)(sy_abs * sy_abs);
+  bool evan;
+  float sv, f;
+  if (ops.phase_fp32) {
+    f = kz_phase_f32(ops.kp, qx, qy, evan, sv);
+  } else {
+    float a_hi, a_lo;
+    column_constant(ops.kp, qx, a_hi, a_lo);
+    f = kz_phase_ff(ops.kp, a_hi, a_lo, qy, evan, sv);
+  }
+  // H = exp(-2*pi*i*f); the adjoint uses conj(H).
+  float2 m = cis_cycles(f, ops.conj ? 1.0f : -1.0f);
+  if (evan) m = ops.evan_mask ? make_float2(0.0f, 0.0f) : make_float2(1.0f, 0.0f);
+  if (ops.dz) {
+    // d/dz exp(-2*pi*i*kz*z) = -2*pi*i*kz * H with kz = k0*sqrt(v).
+    const float gz = ops.kp.two_pi_k0 * sv * (ops.conj ? 1.0f : -1.0f);
+    m = make_float2(-gz * m.y, gz * m.x);
+  }
+  return m;
+}
+
+// Spectral multiply of the thread's 16 points of column kx (rows t + T*j).
+// The transfer function of the tile's C columns is first tabulated in shared
+// memory over |ky| = 0..N/2 (C*(N/2+1) evaluations shared by all threads),
+// then each point reads its entry.  The buffer must be free on entry; it is
+// in use on exit (callers sync before the next transform).
+template <int N, int C>
+__device__ __forceinline__ void apply_spectral(float2 (&v)[16], float2* tab, int x0, int c, int t,
+                                               const ColOps& ops) {
+  constexpr int T = FftGeo<N>::T, NT = C * T, E = (N / 2 + 1) * C;
+  const int kx = x0 + c;
+  if (ops.apply_h) {
+#pragma unroll 1
+    for (int i = threadIdx.x; i < E; i += NT) {
+      const int cc = i % C, a = i / C;
+      const int x = x0 + cc;
+      tab[i] = transfer_value<N>(a, x < N / 2 ? x : x - N, ops);
+    }
+    __syncthreads();
+  }
+  static_for<16>([&](auto jc) {
+    constexpr int j = decltype(jc)::value;
+    const int ky = t + T * j;
+    float2 m = make_float2(1.0f, 0.0f);
+    if (ops.apply_h) {
+      const int a = ky <= N / 2 ? ky : N - ky;
+      m = tab[a * C + c];
+    }
+    if (ops.kmask) {
+      float2 km = mask_value(ops.kmask, ops.kmask_type, (size_t)ky * N + kx);
+      if (ops.conj) km = cconj(km);
+      m = cmul(m, km);
+    }
+    if (ops.apply_h || ops.kmask) v[j] = cmul(v[j], m);
+    if (ops.spectrum_out) ops.spectrum_out[(size_t)ky * N + kx] = v[j];
+    if (ops.scale != 1.0f) v[j] = cscale(v[j], ops.scale);
+  });
+}
+
+template <int N, bool CG = false>
+__device__ __forceinline__ void load_col(float2 (&v)[16], const float2* in, int x, int t) {
+  constexpr int T = FftGeo<N>::T;
+  const float2* src = in + (size_t)t * N + x;
+  static_for<16>([&](auto jc) {
+    v[decltype(jc)::value] = gld<CG>(src + (size_t)T * N * decltype(jc)::value);
+  });
+}
+
+// Column tile: columns tile*C .. tile*C+C-1 by the CTA's first C*T threads,
+// thread (c = threadIdx.x % C, t = threadIdx.x / C).  MODE: COL_FWD forward
+// transform; COL_INV spectral multiply then inverse transform; COL_FUSED
+// forward, spectral multiply, inverse (one copy of the transform code:
+// inverse(x) = conj(forward(conj(x)))).  v holds the thread's loaded points;
+// `after_first` runs after the first stage of the first transform.  The
+// buffer (C * BUF float2) must be free on entry.
+template <int N, int MODE, int C, bool CG, class Hook>
+__device__ __forceinline__ void col_tile(float2 (&v)[16], float2* out, int tile, const ColOps& ops,
+                                         float2* buf, const float2* tw, Hook after_first) {
+  constexpr int T = FftGeo<N>::T;
+  const int c = threadIdx.x % C, t = threadIdx.x / C;
+  const int x0 = tile * C, x = x0 + c;
+  if constexpr (MODE == COL_FWD) {
+    fft_first<N, -1, true, C>(v, buf, t, c);
+    after_first();
+    fft_rest<N, -1, true, C, true>(v, buf, tw, t, c);
+  } else if constexpr (MODE == COL_INV) {
+    apply_spectral<N, C>(v, buf, x0, c, t, ops);
+    __syncthreads();
+    fft_first<N, 1, true, C>(v, buf, t, c);
+    after_first();
+    fft_rest<N, 1, true, C, true>(v, buf, tw, t, c);
+  } else {
+#pragma unroll 1
+    for (int pass = 0; pass < 2; ++pass) {
+      fft_first<N, -1, true, C>(v, buf, t, c);
+      if (pass == 0) after_first();
+      fft_rest<N, -1, true, C, true>(v, buf, tw, t, c);
+      __syncthreads();
+      if (pass == 0) {
+        apply_spectral<N, C>(v, buf, x0, c, t, ops);
+        __syncthreads();
+        conj16(v);
+      }
+    }
+    conj16(v);
+  }
+  float2* dst = out + (size_t)t * N + x;
+  static_for<16>([&](auto jc) {
+    gst<CG>(dst + (size_t)T * N * decltype(jc)::value, v[decltype(jc)::value]);
+  });
+}
+
+struct NoHook {
+  __device__ __forceinline__ void operator()() const {}
+};
+
+}  // namespace lp

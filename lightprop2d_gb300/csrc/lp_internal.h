@@ -52,7 +52,20 @@ struct SizeOps {
   // Resident CTAs per SM for the persistent row (kind 0) / column (kind 1)
   // kernels; 0 restores the built-in choice.  Returns the value in effect.
   int (*set_ctas_per_sm)(int kind, int value);
+  // Device address of this size's stage-twiddle table (valid after init).
+  const float2* (*twiddles)();
 };
+
+// Per-device set-up of the batched persistent kernel (lp_batch.cu).
+cudaError_t batch_init();
+
+// Transfer-function constants for grid n, side `area`, wavelength wl and
+// distance z (all in the caller's length unit).
+KParams make_kparams(int n, double area, double wl, double z);
+// Column-pass ops of a propagate: H(z) (if apply_h) and the lp_flags bits.
+ColOps make_colops(int n, double area, double wl, double z, bool apply_h, uint32_t flags);
+// Thin-lens phase of focal length f folded into a row pass.
+void set_lens(RowOps& o, int n, double area, double wl, double f);
 
 const SizeOps* size_ops(int n);
 

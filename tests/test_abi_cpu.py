@@ -71,3 +71,32 @@ def test_validation_before_any_device_call(lib):
         L.check(L.LP_ERR_OUT_OF_MEMORY, "x")
     with pytest.raises(L.BackendError):
         L.check(L.LP_ERR_CUDA, "x")
+
+
+def test_batch_validation_before_any_device_call(lib):
+    from lightprop2d_gb300 import _lib as L
+    vp = ctypes.c_void_p
+    out = vp()
+
+    def create(descs, opts=None):
+        arr = (L.BeamDesc * max(1, len(descs)))(*descs)
+        return lib.lp_batch_create(arr, len(descs), opts, ctypes.byref(out))
+
+    ok = dict(field=4096, iprofile=0, n=256, area_size=0.2, wl=632e-7, z=1.0, lens_f=0.0,
+              flags=0)
+    assert create([]) == L.LP_ERR_INVALID_ARGUMENT
+    assert create([L.BeamDesc(**{**ok, "n": 100})]) == L.LP_ERR_UNSUPPORTED_SIZE
+    assert create([L.BeamDesc(**{**ok, "n": 32})]) == L.LP_ERR_UNSUPPORTED_SIZE
+    assert create([L.BeamDesc(**ok), L.BeamDesc(**{**ok, "n": 8192})]) == \
+        L.LP_ERR_UNSUPPORTED_SIZE
+    assert b"beam 1" in lib.lp_last_error()
+    assert create([L.BeamDesc(**{**ok, "field": 0})]) == L.LP_ERR_INVALID_ARGUMENT
+    assert create([L.BeamDesc(**{**ok, "field": 4100})]) == L.LP_ERR_MISALIGNED
+    assert create([L.BeamDesc(**{**ok, "iprofile": 4098})]) == L.LP_ERR_MISALIGNED
+    assert create([L.BeamDesc(**{**ok, "wl": 0.0})]) == L.LP_ERR_INVALID_ARGUMENT
+    assert create([L.BeamDesc(**{**ok, "z": float("nan")})]) == L.LP_ERR_INVALID_ARGUMENT
+    assert create([L.BeamDesc(**{**ok, "flags": L.LP_FLAG_ADJOINT})]) == \
+        L.LP_ERR_INVALID_ARGUMENT
+    assert out.value is None
+    assert lib.lp_batch_run(vp(0), vp(0)) == L.LP_ERR_INVALID_ARGUMENT
+    assert lib.lp_batch_status(vp(0), vp(0)) == L.LP_ERR_INVALID_ARGUMENT

@@ -88,6 +88,27 @@ def test_propagate_field_fused(B, n):
     assert np.allclose(host(ip), np.abs(f_ref) ** 2, rtol=1e-4, atol=1e-6 * np.abs(f_ref).max() ** 2)
 
 
+@pytest.mark.parametrize("n,area,wl,z", [
+    (2048, 0.10409037570395337, 1064 * nm, 1.7394964232143395),
+    (2048, 0.04663, 632 * nm, 1.87),
+    (1024, 0.05, 1064 * nm, 3.3),
+    (1024, 0.025, 532 * nm, 12.0),
+    (4096, 0.1, 632 * nm, 5.0),
+    (512, 0.012, 632 * nm, 3.7)])
+def test_near_evanescent_cutoff(B, n, area, wl, z):
+    """White-spectrum fields on grids finer than wl/2 put energy at the
+    evanescent cut-off, where kz*z = R*sqrt(v) with v -> 0 after cancellation;
+    the float-float phase must stay within the bar there too."""
+    g = O.grids(area, n, wl)
+    assert area / n < wl / 2
+    x = O.random_phase_hole(n, area, 0.3 * area, seed=n + 1)
+    _, f_ref = O.propagate(np.fft.fft2(x), g["Kz"], z)
+    out = B.propagate_field(dev(x), area, wl, z)
+    assert O.rel_l2(host(out), f_ref) < TOL
+    s = B.propagate(dev(np.fft.fft2(x)), area, wl, z, write_spectrum=False)
+    assert O.rel_l2(host(s), f_ref) < TOL
+
+
 def test_config2_gaussian_2048_all_z(B):
     """2048^2, 2 mm, 632 nm, waist 100 um, z in {0.1,1,5,10,50} cm.
 
