@@ -3,15 +3,18 @@
 Workload (``config.workload``): Gaussian beam, npoints=2048, area 2 mm,
 wl 632 nm, waist 100 um, complex64, propagated by z = 1 cm per step.  A step
 is one fused field -> field propagate (fft2 -> H(z) in registers -> ifft2,
-read field / write field) with the field resident in HBM; the L2 is flushed
-(a 320 MiB write) before every timed step and the flush is outside the timed
-events.
+read field / write field) with the field resident in HBM.  L2 hygiene: the
+timed steps rotate over in/out grid pairs totalling > 2.5x the L2, so no step
+finds its input in L2 (a 320 MiB-flush variant is reported beside it).
 
-Also reported: the Beam2D.propagate steady state (stored spectrum -> field),
-the plain unfused form (fft2, H grid in HBM, multiply, ifft2) with the
-float-float H and with the reference-literal FP64 H, the plain-FP32-phase
-variant's error, an N sweep (512..4096) and ``e2e``: the same step through
-the C ABI with host buffers (pinned H2D copy, propagate, D2H copy timed).
+Also reported: the per-pass breakdown, the Beam2D.propagate steady state
+(stored spectrum -> field), the plain unfused form (fft2, H grid in HBM,
+multiply, ifft2) with the float-float H and with the reference-literal FP64
+H, the plain-FP32-phase variant's error by z, an N sweep (512..4096), the
+phase-mask inverse design and split-step chain workloads, the 4096-beam
+uneven batch (one persistent launch in a CUDA graph, autotuned, against
+per-beam calls) and ``e2e``: the same step through the C ABI with host
+buffers (pinned H2D copy, propagate, D2H copy timed).
 
 ``--impl reference`` times the reference algorithm (the numpy oracle port of
 beam2d.py:481-490 with the fft2 of the field first) on the host cores, one
@@ -551,6 +554,11 @@ def main():
             "peak_extra_gib": round((torch.cuda.max_memory_allocated() - base) / 2 ** 30, 3),
             "screens_gib": round(screens.numel() * 4 / 2 ** 30, 3)}
         del screens, sc, y, u0
+        torch.cuda.empty_cache()
+
+        # Uneven batch: 4096 beams in one persistent launch (CUDA graph).
+        extra["batch_uneven"] = batch_section(dev, stream, clocks, reps=20)
+        torch.cuda.empty_cache()
 
     # ----------------------------------------------------------------- e2e --
     hin = torch.empty((n, n), dtype=torch.complex64, pin_memory=True)

@@ -95,10 +95,17 @@ lp_status lp_workspace_release(void);
 lp_status lp_profile_events(void** events, int count);
 /* Tuning hook (no counterpart in the reference): resident CTAs per SM for the
  * persistent row (kind 0) or column (kind 1) kernels of size n; value 0
- * restores the built-in choice (the count whose last wave is fullest).
- * Returns the count now in effect, or -1 for a bad n / kind.  Process-wide;
- * set by the autotuner (lightprop2d_gb300.tune), not needed otherwise. */
+ * restores the built-in choice (as many as fit).  The TMA-staged row kernels
+ * (n = 4096, 16-byte aligned input) always run one CTA per SM and ignore
+ * kind 0.  Returns the count now in effect, or -1 for a bad n / kind.
+ * Process-wide; set by the autotuner (lightprop2d_gb300.tune). */
 int lp_tune_ctas_per_sm(int n, int kind, int value);
+/* Health check (no counterpart in the reference): synchronises `stream` and
+ * returns LP_ERR_TIMEOUT if a bounded device-side wait of any pass kernel
+ * (a TMA copy that never landed) gave up since the last call, clearing the
+ * record; LP_OK otherwise.  The pass kernels never hang: a wait that runs
+ * out of iterations records the error and the kernel finishes. */
+lp_status lp_async_status(void* stream);
 
 /* ------------------------------------------------------------ transforms --
  * numpy convention: forward unnormalised, inverse scaled by 1/N^2.

@@ -66,6 +66,7 @@ SIGNATURES = {
     "lp_workspace_release": [],
     "lp_profile_events": [ctypes.POINTER(ctypes.c_void_p), _i],
     "lp_tune_ctas_per_sm": [_i, _i, _i],
+    "lp_async_status": [_vp],
     "lp_fft2": [_vp, _vp, _i, _i, _vp],
     "lp_propagate": [_vp, _vp, _i, _d, _d, _d, _vp, _i, _u, _vp],
     "lp_propagate_field": [_vp, _vp, _vp, _vp, _i, _d, _d, _d, _d, _vp, _i, _vp, _i,

@@ -1,0 +1,78 @@
+// Bulk asynchronous copies (TMA engine) and shared-memory mbarriers, as
+// inline PTX for sm_100-class GPUs.
+//
+// A landing slot in shared memory has one mbarrier.  The producing thread
+// arms it with the byte count of the copy (arrive.expect_tx) and issues
+// cp.async.bulk; the barrier's phase completes when the bytes have landed.
+// Consumers wait on the phase parity with a bounded loop: if the limit runs
+// out the wait records an error flag and returns false instead of hanging.
+#pragma once
+
+#include <cstdint>
+
+namespace lp {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+// Makes barrier initialisation visible to the async proxy (before any copy).
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Orders this thread's earlier generic-proxy shared-memory accesses before
+// later async-proxy (bulk copy) accesses.
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Arms `bar` for `bytes` and copies `bytes` (multiple of 16; both addresses
+// 16-byte aligned) from global `src` to shared `dst`.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes,
+                                          uint64_t* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n"
+      "  .reg .pred p;\n"
+      "  mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "  selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Default iteration limit of a bounded wait (each try_wait may also suspend
+// the thread for a short, hardware-chosen time).
+constexpr long long kWaitLimit = 1LL << 24;
+
+// Waits for the phase of parity `parity` of `bar`; false (and *err = 1) if the
+// limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err,
+                                          long long limit = kWaitLimit) {
+#pragma unroll 1
+  for (long long k = 0; k < limit; ++k)
+    if (mbar_try_wait(bar, parity)) return true;
+  atomicExch(err, 1);
+  return false;
+}
+
+}  // namespace lp

@@ -401,6 +401,19 @@ lp_status lp_workspace_release(void) {
   return r;
 }
 
+lp_status lp_async_status(void* stream) {
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "lp_async_status: synchronize");
+  int bad = 0;
+  for (int n = 16; n <= 4096; n *= 2) {
+    const int r = size_ops(n)->take_async_error();
+    if (r < 0) return fail(LP_ERR_CUDA, "lp_async_status: reading the error record failed");
+    bad |= r;
+  }
+  if (bad) return fail(LP_ERR_TIMEOUT, "a bounded device-side wait gave up (TMA copy never landed)");
+  return LP_OK;
+}
+
 lp_status lp_profile_events(void** events, int count) {
   if (count < 0 || count > 8 || (count > 0 && !events))
     return fail(LP_ERR_INVALID_ARGUMENT, "lp_profile_events: 0 <= count <= 8 events");

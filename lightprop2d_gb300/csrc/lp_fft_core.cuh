@@ -88,9 +88,26 @@ __device__ __forceinline__ int sidx(int i, int line) {
   else return line * FftGeo<N>::BUF + pad16(i);
 }
 
-template <bool CTA>
-__device__ __forceinline__ void line_sync() {
-  if constexpr (CTA) __syncthreads(); else __syncwarp();
+// Barrier over the threads that share an exchange buffer.  SY = 0: the warp
+// (lines of <= 32 threads); SY = 1: the whole CTA; SY = 2: the calling
+// thread's group of 256 threads (named barrier 1 + threadIdx.x / 256), for
+// kernels whose CTA holds several independent tile groups.
+template <int SY>
+__device__ __forceinline__ void group_sync() {
+  if constexpr (SY == 0) {
+    __syncwarp();
+  } else if constexpr (SY == 1) {
+    __syncthreads();
+  } else {
+    asm volatile("bar.sync %0, 256;" ::"r"(1 + (int)(threadIdx.x >> 8)) : "memory");
+  }
+}
+
+// Thread index within the exchange group.
+template <int SY>
+__device__ __forceinline__ int group_tid() {
+  if constexpr (SY == 2) return (int)(threadIdx.x & 255u);
+  else return (int)threadIdx.x;
 }
 
 // Global loads / stores; CG = cache at L2 only (data produced by other CTAs
@@ -119,7 +136,7 @@ __device__ __forceinline__ void fft_first(float2 (&v)[16], float2* buf, int t, i
 
 // Stage s > 0: inputs from shared memory, twiddled, DFT, outputs to shared
 // memory (middle stage) or to registers in natural order (last stage).
-template <int N, int S, int s, bool IL, int LINES, bool CTA>
+template <int N, int S, int s, bool IL, int LINES, int SY>
 __device__ __forceinline__ void fft_stage(float2 (&v)[16], float2* buf, const float2* tw, int t,
                                           int line) {
   using G = FftGeo<N>;
@@ -127,7 +144,7 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[16], float2* buf, const fl
   constexpr int NS = (s == 1) ? G::NS1 : G::NS2;
   constexpr int OFF = (s == 1) ? G::TW_OFF1 : G::TW_OFF2;
   constexpr bool LAST = (s == G::NST - 1);
-  line_sync<CTA>();
+  group_sync<SY>();
   static_for<nb>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
     const int b = t + q * T;
@@ -136,7 +153,7 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[16], float2* buf, const fl
       v[q + nb * r] = buf[sidx<N, IL, LINES>(b + r * (N / R), line)];
     });
   });
-  if constexpr (!LAST) line_sync<CTA>();
+  if constexpr (!LAST) group_sync<SY>();
   static_for<nb>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
     const int b = t + q * T;
@@ -164,11 +181,11 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[16], float2* buf, const fl
 
 // Stages after the first (natural-order result in registers).  tw: the
 // stage twiddles of size N (shared memory).
-template <int N, int S, bool IL, int LINES, bool CTA>
+template <int N, int S, bool IL, int LINES, int SY>
 __device__ __forceinline__ void fft_rest(float2 (&v)[16], float2* buf, const float2* tw, int t,
                                          int line) {
-  if constexpr (FftGeo<N>::NST >= 2) fft_stage<N, S, 1, IL, LINES, CTA>(v, buf, tw, t, line);
-  if constexpr (FftGeo<N>::NST == 3) fft_stage<N, S, 2, IL, LINES, CTA>(v, buf, tw, t, line);
+  if constexpr (FftGeo<N>::NST >= 2) fft_stage<N, S, 1, IL, LINES, SY>(v, buf, tw, t, line);
+  if constexpr (FftGeo<N>::NST == 3) fft_stage<N, S, 2, IL, LINES, SY>(v, buf, tw, t, line);
 }
 
 __device__ __forceinline__ void conj16(float2 (&v)[16]) {
@@ -192,11 +209,11 @@ __device__ __forceinline__ float2 xop_value(int y, int x, const RowOps& ops) {
 // Multiply the thread's 16 points of row y by the x-domain multiplier,
 // evaluated in a rolled loop into the thread's own buffer slots (one copy of
 // the phase code), then applied.  The slots must be free.
-template <int N>
+template <int N, int SY = 1>
 __device__ __forceinline__ void apply_xops(float2 (&v)[16], float2* slots, int nthreads, int y,
                                            int t, const RowOps& ops) {
   constexpr int T = FftGeo<N>::T;
-  const int tid = threadIdx.x;
+  const int tid = group_tid<SY>();
 #pragma unroll 1
   for (int j = 0; j < 16; ++j) slots[j * nthreads + tid] = xop_value<N>(y, t + T * j, ops);
   static_for<16>([&](auto jc) {
@@ -212,32 +229,34 @@ __device__ __forceinline__ void load_row(float2 (&v)[16], const float2* in, int 
   static_for<16>([&](auto jc) { v[decltype(jc)::value] = gld<CG>(src + T * decltype(jc)::value); });
 }
 
-// Row tile: rows tile*L .. tile*L+L-1 by the CTA's first L*T threads, thread
-// (line g = threadIdx.x / T, t = threadIdx.x % T).  v holds the thread's
-// loaded points of row tile*L + g; `after_first` runs after the first stage
-// (the per-size kernels prefetch the next tile there).  The exchange buffer
-// (L * BUF floats2) must be free on entry.
-template <int N, int S, int L, int NT, bool CG, class Hook>
+// Row tile: rows tile*L .. tile*L+L-1 by the first L*T threads of the
+// exchange group (SY: the CTA, or a 256-thread group), thread (line
+// g = tid / T, t = tid % T).  v holds the thread's loaded points of row
+// tile*L + g; `after_first` runs after the first stage (the per-size kernels
+// prefetch the next tile there).  The exchange buffer (L * BUF floats2) must
+// be free on entry.
+template <int N, int S, int L, int NT, bool CG, int SY = 1, class Hook>
 __device__ __forceinline__ void row_tile(float2 (&v)[16], float2* out, int tile, const RowOps& ops,
                                          float2* buf, const float2* tw, Hook after_first) {
   constexpr int T = FftGeo<N>::T;
-  constexpr bool CTA = T > 32;
-  const int g = threadIdx.x / T, t = threadIdx.x % T;
+  constexpr int LS = T > 32 ? SY : 0;  // a line spans several warps
+  const int tid = group_tid<SY>();
+  const int g = tid / T, t = tid % T;
   const int y = tile * L + g;
   const bool xops = ops.lens || ops.xmask;
   if (xops && !ops.x_at_store) {
-    apply_xops<N>(v, buf, NT, y, t, ops);
-    __syncthreads();
+    apply_xops<N, SY>(v, buf, NT, y, t, ops);
+    group_sync<SY>();
   }
   fft_first<N, S, false, L>(v, buf, t, g);
   after_first();
-  fft_rest<N, S, false, L, CTA>(v, buf, tw, t, g);
+  fft_rest<N, S, false, L, LS>(v, buf, tw, t, g);
   if (ops.scale != 1.0f) {
     static_for<16>([&](auto jc) { v[decltype(jc)::value] = cscale(v[decltype(jc)::value], ops.scale); });
   }
   if (xops && ops.x_at_store) {
-    __syncthreads();
-    apply_xops<N>(v, buf, NT, y, t, ops);
+    group_sync<SY>();
+    apply_xops<N, SY>(v, buf, NT, y, t, ops);
   }
   float2* dst = out + (size_t)y * N + t;
   static_for<16>([&](auto jc) { gst<CG>(dst + T * decltype(jc)::value, v[decltype(jc)::value]); });
@@ -280,19 +299,19 @@ __device__ __forceinline__ float2 transfer_value(int sy_abs, int sx, const ColOp
 // memory over |ky| = 0..N/2 (C*(N/2+1) evaluations shared by all threads),
 // then each point reads its entry.  The buffer must be free on entry; it is
 // in use on exit (callers sync before the next transform).
-template <int N, int C>
+template <int N, int C, int SY = 1>
 __device__ __forceinline__ void apply_spectral(float2 (&v)[16], float2* tab, int x0, int c, int t,
                                                const ColOps& ops) {
   constexpr int T = FftGeo<N>::T, NT = C * T, E = (N / 2 + 1) * C;
   const int kx = x0 + c;
   if (ops.apply_h) {
 #pragma unroll 1
-    for (int i = threadIdx.x; i < E; i += NT) {
+    for (int i = group_tid<SY>(); i < E; i += NT) {
       const int cc = i % C, a = i / C;
       const int x = x0 + cc;
       tab[i] = transfer_value<N>(a, x < N / 2 ? x : x - N, ops);
     }
-    __syncthreads();
+    group_sync<SY>();
   }
   static_for<16>([&](auto jc) {
     constexpr int j = decltype(jc)::value;
@@ -322,39 +341,40 @@ __device__ __forceinline__ void load_col(float2 (&v)[16], const float2* in, int 
   });
 }
 
-// Column tile: columns tile*C .. tile*C+C-1 by the CTA's first C*T threads,
-// thread (c = threadIdx.x % C, t = threadIdx.x / C).  MODE: COL_FWD forward
+// Column tile: columns tile*C .. tile*C+C-1 by the first C*T threads of the
+// exchange group (SY), thread (c = tid % C, t = tid / C).  MODE: COL_FWD forward
 // transform; COL_INV spectral multiply then inverse transform; COL_FUSED
 // forward, spectral multiply, inverse (one copy of the transform code:
 // inverse(x) = conj(forward(conj(x)))).  v holds the thread's loaded points;
 // `after_first` runs after the first stage of the first transform.  The
 // buffer (C * BUF float2) must be free on entry.
-template <int N, int MODE, int C, bool CG, class Hook>
+template <int N, int MODE, int C, bool CG, int SY = 1, class Hook>
 __device__ __forceinline__ void col_tile(float2 (&v)[16], float2* out, int tile, const ColOps& ops,
                                          float2* buf, const float2* tw, Hook after_first) {
   constexpr int T = FftGeo<N>::T;
-  const int c = threadIdx.x % C, t = threadIdx.x / C;
+  const int tid = group_tid<SY>();
+  const int c = tid % C, t = tid / C;
   const int x0 = tile * C, x = x0 + c;
   if constexpr (MODE == COL_FWD) {
     fft_first<N, -1, true, C>(v, buf, t, c);
     after_first();
-    fft_rest<N, -1, true, C, true>(v, buf, tw, t, c);
+    fft_rest<N, -1, true, C, SY>(v, buf, tw, t, c);
   } else if constexpr (MODE == COL_INV) {
-    apply_spectral<N, C>(v, buf, x0, c, t, ops);
-    __syncthreads();
+    apply_spectral<N, C, SY>(v, buf, x0, c, t, ops);
+    group_sync<SY>();
     fft_first<N, 1, true, C>(v, buf, t, c);
     after_first();
-    fft_rest<N, 1, true, C, true>(v, buf, tw, t, c);
+    fft_rest<N, 1, true, C, SY>(v, buf, tw, t, c);
   } else {
 #pragma unroll 1
     for (int pass = 0; pass < 2; ++pass) {
       fft_first<N, -1, true, C>(v, buf, t, c);
       if (pass == 0) after_first();
-      fft_rest<N, -1, true, C, true>(v, buf, tw, t, c);
-      __syncthreads();
+      fft_rest<N, -1, true, C, SY>(v, buf, tw, t, c);
+      group_sync<SY>();
       if (pass == 0) {
-        apply_spectral<N, C>(v, buf, x0, c, t, ops);
-        __syncthreads();
+        apply_spectral<N, C, SY>(v, buf, x0, c, t, ops);
+        group_sync<SY>();
         conj16(v);
       }
     }

@@ -9,6 +9,7 @@
 // scheduled as this pass retires.
 #pragma once
 
+#include "lp_async.cuh"
 #include "lp_fft_core.cuh"
 
 #ifndef LP_N
@@ -18,10 +19,34 @@
 #ifndef LP_COL_C
 #define LP_COL_C 4
 #endif
+// Per-size choices below were measured on GB300 (fused propagate, inputs
+// larger than L2); each can be overridden with -D for tuning experiments.
 // 1: load the next tile into a second register set while transforming the
 // current one; 0: load it at the top of the next iteration.
-#ifndef LP_PREFETCH
-#define LP_PREFETCH 1
+#ifndef LP_ROW_PREFETCH
+#define LP_ROW_PREFETCH 1
+#endif
+#ifndef LP_COL_PREFETCH
+#define LP_COL_PREFETCH (LP_N >= 4096)
+#endif
+// Minimum resident CTAs per SM requested from the register allocator
+// (2 with 512-thread column CTAs caps them at 64 registers).
+#ifndef LP_ROW_MINB
+#define LP_ROW_MINB 1
+#endif
+#ifndef LP_COL_MINB
+#define LP_COL_MINB (LP_N >= 4096 ? 1 : 2)
+#endif
+// TMA-staged row kernels (1) or register-prefetch kernels (0); used for
+// N >= 1024 only.  TMA wins at 4096 (rows of 32 KB); at 1024-2048 the
+// register kernels, which use every SM, are faster.
+#ifndef LP_ROW_TMA
+#define LP_ROW_TMA (LP_N >= 4096)
+#endif
+// TMA row kernels: equal contiguous tile runs per group on as many SMs as
+// that needs (1), or tiles strided over every SM (0).
+#ifndef LP_TMA_BALANCED
+#define LP_TMA_BALANCED 1
 #endif
 
 namespace lp {
@@ -55,7 +80,7 @@ __device__ __forceinline__ void load_twiddles(float2* dst) {
 }
 
 template <int N, int S>
-__global__ void __launch_bounds__(Geo<N>::ROW_THREADS)
+__global__ void __launch_bounds__(Geo<N>::ROW_THREADS, LP_ROW_MINB)
     row_kernel(const float2* in, float2* out, RowOps ops) {
   constexpr int T = Geo<N>::T, L = Geo<N>::ROWS, NU = Geo<N>::ROW_UNITS;
   constexpr int NT = Geo<N>::ROW_THREADS;
@@ -67,18 +92,18 @@ __global__ void __launch_bounds__(Geo<N>::ROW_THREADS)
   pdl_release();
   int tile = blockIdx.x;
   float2 v[16];
-#if LP_PREFETCH
+#if LP_ROW_PREFETCH
   float2 p[16];
   if (tile < NU) load_row<N>(v, in, tile * L + g, t);
 #endif
 #pragma unroll 1
   while (tile < NU) {
     const int next = tile + gridDim.x;
-#if !LP_PREFETCH
+#if !LP_ROW_PREFETCH
     load_row<N>(v, in, tile * L + g, t);
 #endif
     __syncthreads();  // buffer free: previous tile's last-stage reads are done
-#if LP_PREFETCH
+#if LP_ROW_PREFETCH
     row_tile<N, S, L, NT, false>(v, out, tile, ops, smem, tw, [&] {
       if (next < NU) load_row<N>(p, in, next * L + g, t);
     });
@@ -91,7 +116,7 @@ __global__ void __launch_bounds__(Geo<N>::ROW_THREADS)
 }
 
 template <int N, int MODE>
-__global__ void __launch_bounds__(Geo<N>::COL_THREADS)
+__global__ void __launch_bounds__(Geo<N>::COL_THREADS, LP_COL_MINB)
     col_kernel(const float2* in, float2* out, ColOps ops) {
   constexpr int T = Geo<N>::T, C = Geo<N>::COLS, NU = Geo<N>::COL_UNITS;
   extern __shared__ float2 smem[];
@@ -102,18 +127,18 @@ __global__ void __launch_bounds__(Geo<N>::COL_THREADS)
   pdl_release();
   int tile = blockIdx.x;
   float2 v[16];
-#if LP_PREFETCH
+#if LP_COL_PREFETCH
   float2 p[16];
   if (tile < NU) load_col<N>(v, in, tile * C + c, t);
 #endif
 #pragma unroll 1
   while (tile < NU) {
     const int next = tile + gridDim.x;
-#if !LP_PREFETCH
+#if !LP_COL_PREFETCH
     load_col<N>(v, in, tile * C + c, t);
 #endif
     __syncthreads();  // buffer free: previous tile's last-stage reads are done
-#if LP_PREFETCH
+#if LP_COL_PREFETCH
     col_tile<N, MODE, C, false>(v, out, tile, ops, smem, tw, [&] {
       if (next < NU) load_col<N>(p, in, next * C + c, t);
     });
@@ -122,6 +147,95 @@ __global__ void __launch_bounds__(Geo<N>::COL_THREADS)
     col_tile<N, MODE, C, false>(v, out, tile, ops, smem, tw, NoHook{});
 #endif
     tile = next;
+  }
+}
+
+// ------------------------------------------------------ TMA-staged rows --
+// Set when a bounded wait of this size's kernels gave up (read and cleared by
+// take_async_error on the host).
+__device__ int g_async_err;
+
+// Row pass for N >= 1024 on 16-byte aligned grids.  One CTA per SM holds two
+// independent groups of 256 threads.  A tile is 4096 points (4096/N whole
+// rows, contiguous in memory); each group owns a contiguous run of `tpg`
+// tiles and SL landing slots that the TMA engine fills with one bulk copy per
+// tile.  A group reads a landed tile into registers, hands the slot straight
+// back to the copy engine for its tile SL ahead, and transforms in its own
+// exchange buffer, so up to 2*SL tiles per SM are in flight while the SM
+// computes, and no registers are spent on prefetching.  The grid is sized so
+// every group gets the same number of tiles (a memory-bound pass is balanced
+// by its copies in flight, not by using every SM).
+template <int N>
+struct RowTma {
+  static constexpr int TILE = 4096;
+  static constexpr int L = TILE / N;
+  static constexpr int G = 2;
+  static constexpr int SL = N >= 4096 ? 1 : 2;
+  static constexpr int NU = N / L;
+  static constexpr size_t XBUF = (size_t)L * FftGeo<N>::BUF;         // float2 per group
+  static constexpr size_t OFF_LAND = G * XBUF;                        // float2
+  static constexpr size_t OFF_TW = OFF_LAND + (size_t)G * SL * TILE;  // float2
+  static constexpr size_t BAR_BYTES =
+      ((OFF_TW + FftGeo<N>::TW_SIZE) * sizeof(float2) + 15) / 16 * 16;
+  static constexpr size_t SMEM = BAR_BYTES + G * SL * sizeof(uint64_t);
+};
+
+template <int N, int S>
+__global__ void __launch_bounds__(512, 1)
+    row_kernel_tma(const float2* in, float2* out, RowOps ops, int tpg) {
+  using RT = RowTma<N>;
+  constexpr int T = FftGeo<N>::T, L = RT::L, SL = RT::SL, TILE = RT::TILE;
+  constexpr uint32_t BYTES = TILE * sizeof(float2);
+  extern __shared__ __align__(16) float2 smem[];
+  const int grp = threadIdx.x >> 8, lt = threadIdx.x & 255;
+  float2* xbuf = smem + grp * RT::XBUF;
+  float2* land = smem + RT::OFF_LAND + (size_t)grp * SL * TILE;
+  float2* tw = smem + RT::OFF_TW;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<char*>(smem) + RT::BAR_BYTES);
+  load_twiddles<512>(tw);
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < RT::G * SL; ++k) mbar_init(bars + k, 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  bars += grp * SL;
+#if LP_TMA_BALANCED
+  // tiles first .. first+count-1 (count <= 0 for idle groups of the last CTA)
+  const int first = (blockIdx.x * RT::G + grp) * tpg, step = 1;
+  const int count = min(tpg, RT::NU - first);
+#else
+  // tiles first, first+step, ... over the whole grid
+  const int first = blockIdx.x * RT::G + grp, step = gridDim.x * RT::G;
+  const int count = first < RT::NU ? (RT::NU - 1 - first) / step + 1 : 0;
+#endif
+  pdl_wait();
+  pdl_release();
+  if (lt == 0) {
+    for (int k = 0; k < SL && k < count; ++k)
+      bulk_load(land + k * TILE, in + (size_t)(first + k * step) * TILE, BYTES, bars + k);
+  }
+  const int g = lt / T, t = lt % T;
+  bool ok = true;
+#pragma unroll 1
+  for (int j = 0; j < count; ++j) {
+    const int k = j % SL;
+    ok = mbar_wait(bars + k, (j / SL) & 1, &g_async_err) && ok;
+    float2 v[16];
+    const float2* src = land + k * TILE + g * N + t;
+    static_for<16>([&](auto jc) { v[decltype(jc)::value] = src[T * decltype(jc)::value]; });
+    group_sync<2>();  // slot k read by the whole group; exchange buffer free
+    if (lt == 0 && j + SL < count) {
+      fence_proxy_async();
+      bulk_load(land + k * TILE, in + (size_t)(first + (j + SL) * step) * TILE, BYTES, bars + k);
+    }
+    row_tile<N, S, L, 256, false, 2>(v, out, first + j * step, ops, xbuf, tw, NoHook{});
+  }
+  if (!ok && lt == 0) {
+    // A wait gave up: let each slot's last copy land (bounded) before exit.
+    for (int k = 0; k < SL && k < count; ++k) {
+      const int jl = k + ((count - 1 - k) / SL) * SL;
+      mbar_wait(bars + k, (jl / SL) & 1, &g_async_err);
+    }
   }
 }
 
@@ -172,6 +286,15 @@ cudaError_t init_size() {
     e = cudaFuncSetAttribute(row_kernel<N, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(row_kernel<N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs);
+  if constexpr (N >= 1024) {
+    const int ts = (int)RowTma<N>::SMEM;
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(row_kernel_tma<N, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               ts);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(row_kernel_tma<N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               ts);
+  }
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(col_kernel<N, COL_FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
   if (e == cudaSuccess)
@@ -194,6 +317,16 @@ cudaError_t init_size() {
 cudaError_t launch_row(int inverse, const float2* in, float2* out, const RowOps& ops,
                        cudaStream_t st) {
   constexpr int N = LP_N;
+  if constexpr (N >= 1024 && LP_ROW_TMA) {
+    if ((reinterpret_cast<uintptr_t>(in) & 15u) == 0) {
+      using RT = RowTma<N>;
+      const int tpg = (RT::NU + RT::G * g_sms - 1) / (RT::G * g_sms);
+      const int grid = LP_TMA_BALANCED ? (RT::NU + RT::G * tpg - 1) / (RT::G * tpg)
+                                       : cmin(g_sms, (RT::NU + RT::G - 1) / RT::G);
+      return launch_pdl(inverse ? row_kernel_tma<N, 1> : row_kernel_tma<N, -1>, grid, 512,
+                        RT::SMEM, st, in, out, ops, tpg);
+    }
+  }
   const int grid = grid_for(Geo<N>::ROW_UNITS, g_occ_row, g_ctas_row);
   if (inverse)
     return launch_pdl(row_kernel<N, 1>, grid, Geo<N>::ROW_THREADS, Geo<N>::ROW_SMEM, st, in, out,
@@ -222,6 +355,16 @@ int set_ctas_per_sm(int kind, int value) {
   return ctas_in_effect(occ, slot);
 }
 
+int take_async_error() {
+  int v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_async_err, sizeof(int)) != cudaSuccess) return -1;
+  if (v) {
+    const int zero = 0;
+    if (cudaMemcpyToSymbol(g_async_err, &zero, sizeof(int)) != cudaSuccess) return -1;
+  }
+  return v ? 1 : 0;
+}
+
 const float2* twiddles_dev() {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
@@ -236,5 +379,6 @@ const float2* twiddles_dev() {
 namespace lp {
 extern const SizeOps LP_CAT(size_ops_, LP_N);
 const SizeOps LP_CAT(size_ops_, LP_N) = {LP_N, &init_size, &launch_row, &launch_col,
-                                         &set_ctas_per_sm, &twiddles_dev};
+                                         &set_ctas_per_sm, &twiddles_dev,
+                                         &take_async_error};
 }  // namespace lp

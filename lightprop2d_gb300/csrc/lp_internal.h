@@ -54,6 +54,9 @@ struct SizeOps {
   int (*set_ctas_per_sm)(int kind, int value);
   // Device address of this size's stage-twiddle table (valid after init).
   const float2* (*twiddles)();
+  // 1 if a bounded device-side wait of this size's kernels gave up since the
+  // last call (the flag is cleared), 0 if not, -1 on a CUDA error.
+  int (*take_async_error)();
 };
 
 // Per-device set-up of the batched persistent kernel (lp_batch.cu).

@@ -200,6 +200,43 @@ def test_iprofile_and_apply_transfer(B):
     assert O.rel_l2(host(s), x * O.transfer(g["Kz"], z)) < TOL
 
 
+@pytest.mark.parametrize("n", [1024, 2048, 4096])
+def test_tma_and_register_row_paths_agree(B, n):
+    """At 4096, 16-byte aligned grids take the TMA-staged row kernels and a
+    grid that is only 8-byte aligned takes the register-prefetch kernels
+    (which every grid of 1024-2048 uses).  All match the oracle, in place and
+    out of place, and no bounded wait gave up."""
+    from lightprop2d_gb300 import _lib as L
+    area, wl, z, f = 1 * mm, 632 * nm, 2.0, 4.0
+    g = O.grids(area, n, wl)
+    x = rand_field(n, 3 * n)
+    fl, _ = O.lens(x, g["X"], g["Y"], g["k0"], f)
+    _, f_ref = O.propagate(np.fft.fft2(fl), g["Kz"], z)
+    a = dev(x)
+    assert a.data_ptr() % 16 == 0
+    raw = torch.empty(n * n + 1, dtype=torch.complex64, device="cuda")
+    b = raw[1:].view(n, n)
+    assert b.data_ptr() % 16 == 8
+    b.copy_(a)
+    ip = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    out_a = B.propagate_field(a, area, wl, z, lens_f=f, iprofile_out=ip)
+    out_b = B.propagate_field(b, area, wl, z, lens_f=f)
+    assert O.rel_l2(host(out_a), f_ref) < TOL
+    assert O.rel_l2(host(out_b), f_ref) < TOL
+    assert np.allclose(host(ip), np.abs(host(out_a)) ** 2, rtol=1e-5, atol=1e-7)
+    B.propagate_field(a, area, wl, z, out=a, lens_f=f)      # in place
+    assert O.rel_l2(host(a), f_ref) < TOL
+    s = B.fft2(dev(x))
+    assert O.rel_l2(host(s), np.fft.fft2(x)) < FFT_TOL
+    st = torch.cuda.current_stream()
+    L.check(L.load().lp_async_status(ctypes_vp(st.cuda_stream)), "lp_async_status")
+
+
+def ctypes_vp(v):
+    import ctypes
+    return ctypes.c_void_p(v)
+
+
 def test_errors_are_raised(B):
     with pytest.raises(ValueError):
         B.fft2(torch.zeros((100, 100), dtype=torch.complex64, device="cuda"))
