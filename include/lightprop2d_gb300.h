@@ -62,7 +62,18 @@ typedef enum lp_mask_type {
   LP_MASK_U8 = 3,         /* bool / uint8 (0 or 1) */
   LP_MASK_PHASE_F32 = 4,  /* float32 phase phi in radians: multiplier exp(i*phi) */
   LP_MASK_F64 = 5,        /* real float64 multiplier (numpy default dtype) */
-  LP_MASK_C128 = 6        /* complex128 multiplier, rounded to complex64 */
+  LP_MASK_C128 = 6,       /* complex128 multiplier, rounded to complex64 */
+  /* Compact profile generators, evaluated inside the pass that applies them
+   * (no N x N mask in memory).  The pointer is a device array of 2*N values:
+   *   LP_MASK_SEP_F32:  float32 fx[N], fy[N];  multiplier fx[ix] * fy[iy]
+   *                     (separable profiles: gaussian_beam, rectangle_hole,
+   *                     square_hole, square_slits, plane_wave)
+   *   LP_MASK_SPAN_I32: int32 lo[N], hi[N];    multiplier 1 if lo[ix] <= iy < hi[ix]
+   *                     else 0 (round_hole); x-domain masks only.
+   * The host builds the tables with the reference's own float64 arithmetic
+   * (lightprop2d_gb300/generators.py), so boolean edges match it exactly. */
+  LP_MASK_SEP_F32 = 7,
+  LP_MASK_SPAN_I32 = 8
 } lp_mask_type;
 
 /* Flags (bitwise OR). */
@@ -170,11 +181,39 @@ lp_status lp_spectral_filter(lp_cfloat* spectrum, lp_cfloat* field_out, int n,
 
 /* Beam2D.iprofile (beam2d.py:717): out = |field|^2 as float32. */
 lp_status lp_iprofile(const lp_cfloat* field, float* out, int n, void* stream);
+/* Intensity moments for Beam2D.centroid / D4sigma / centroid_intensity
+ * (beam2d.py:669-752).  Writes 5 doubles to device memory `moments`, with
+ * I = |field|^2, jx = ix - n/2, jy = iy - n/2 (grid-index offsets):
+ *   [0] sum I   [1] sum jx*I   [2] sum jy*I
+ *   [3] sum (jx - xc)^2 I   [4] sum (jy - yc)^2 I,   xc = [1]/[0], yc = [2]/[0]
+ * so Xc = dL*[1]/[0], D4sigma_x = 4*dL*sqrt([3]/[0]).  Two read-only passes
+ * (the second moments about the centroid, like the reference); asynchronous. */
+lp_status lp_beam_moments(const lp_cfloat* field, int n, double* moments, void* stream);
 
 /* spectrum *= H(z) only (no transform): used to materialise a spectrum whose
  * propagation distance the caller kept pending. */
 lp_status lp_apply_transfer(lp_cfloat* spectrum, int n, double area_size,
                             double wl, double z, uint32_t flags, void* stream);
+
+/* ------------------------------------------------------- grid management --
+ * One gather kernel each over the output grid (no spectrum: recompute it with
+ * lp_fft2, as the reference does after each of these). */
+/* Beam2D.expand (beam2d.py:375-404): out (n_out x n_out) is `in` padded by
+ * (n_out - n_in)/2 points on every side, each pad point a copy of the nearest
+ * edge point.  n_out >= n_in, even difference; in != out. */
+lp_status lp_expand(const lp_cfloat* in, int n_in, lp_cfloat* out, int n_out, void* stream);
+/* Beam2D.coarse (beam2d.py:434-460): out (n_in/order squared) is the mean of
+ * each order x order block of `in`.  order divides n_in; in != out. */
+lp_status lp_coarse(const lp_cfloat* in, int n_in, lp_cfloat* out, int order, void* stream);
+/* Beam2D.crop (beam2d.py:406-432): resamples the central window
+ * in[first .. first+n_keep)^2 (window axis coordinates x0 + k*dL_in) onto the
+ * centred grid (j - n_out/2)*dL_out, j < n_out, by bilinear interpolation with
+ * nearest-point values outside the window -- what the reference's
+ * scipy.interpolate.interp2d(kind="linear") does; in != out.  Also serves
+ * Beam2D.lens_image (beam2d.py:513-537), whose sample grid is the field grid
+ * scaled by -l1/l2 (dL_out may then differ in sign from dL_in). */
+lp_status lp_crop(const lp_cfloat* in, int n_in, int first, int n_keep, double x0, double dL_in,
+                  lp_cfloat* out, int n_out, double dL_out, void* stream);
 
 /* ------------------------------------------------------------- batches --
  * Many beams of uneven grid sizes in ONE persistent launch.  Each beam runs

@@ -30,6 +30,8 @@ LP_MASK_U8 = 3
 LP_MASK_PHASE_F32 = 4
 LP_MASK_F64 = 5
 LP_MASK_C128 = 6
+LP_MASK_SEP_F32 = 7
+LP_MASK_SPAN_I32 = 8
 
 # flags
 LP_FLAG_PHASE_FP32 = 0x1
@@ -75,6 +77,10 @@ SIGNATURES = {
     "lp_coordinate_filter": [_vp, _vp, _i, _vp, _i, _vp],
     "lp_spectral_filter": [_vp, _vp, _i, _vp, _i, _vp],
     "lp_iprofile": [_vp, _vp, _i, _vp],
+    "lp_beam_moments": [_vp, _i, _vp, _vp],
+    "lp_expand": [_vp, _i, _vp, _i, _vp],
+    "lp_coarse": [_vp, _i, _vp, _i, _vp],
+    "lp_crop": [_vp, _i, _i, _i, _d, _d, _vp, _i, _d, _vp],
     "lp_apply_transfer": [_vp, _i, _d, _d, _d, _u, _vp],
     "lp_plain_propagate_field": [_vp, _vp, _i, _d, _d, _d, _u, _vp],
     "lp_plain_propagate_field_noalloc": [_vp, _vp, _i, _d, _d, _d, _u, _vp],

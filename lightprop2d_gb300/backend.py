@@ -54,6 +54,10 @@ def mask_arg(mask, n: int, device, name="mask", phase: bool = False):
     """
     if mask is None:
         return None, L.LP_MASK_NONE
+    if hasattr(mask, "code") and hasattr(mask, "table"):  # generators.GenMask
+        if mask.table.numel() != 2 * n or mask.table.device != torch.device(device):
+            raise ValueError(f"{name}: compact generator table for a different grid")
+        return mask.table, mask.code
     if isinstance(mask, np.ndarray):
         if mask.dtype == np.bool_:
             mask = torch.from_numpy(mask.astype(np.uint8))
@@ -186,6 +190,47 @@ def iprofile(field: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tens
     out = torch.empty((n, n), dtype=torch.float32, device=field.device) if out is None else out
     _grid(out, "out", torch.float32)
     _call("lp_iprofile", field.device, _vp(field), _vp(out), n)
+    return out
+
+
+def beam_moments(field: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+    """Intensity moments (5 float64 on the device): sum I, sum jx I, sum jy I,
+    sum (jx-xc)^2 I, sum (jy-yc)^2 I with grid-index offsets jx = ix - n/2
+    (lp_beam_moments; Beam2D.centroid / D4sigma, beam2d.py:669-704)."""
+    n = _grid(field, "field")
+    out = torch.empty(5, dtype=torch.float64, device=field.device) if out is None else out
+    if out.dtype != torch.float64 or out.numel() < 5 or not out.is_cuda:
+        raise ValueError("out: float64 CUDA tensor of 5 elements")
+    _call("lp_beam_moments", field.device, _vp(field), n, _vp(out))
+    return out
+
+
+def expand(field: torch.Tensor, n_out: int) -> torch.Tensor:
+    """Edge-replicated padding to n_out x n_out (lp_expand; beam2d.py:375-404)."""
+    n = _grid(field, "field")
+    out = torch.empty((n_out, n_out), dtype=torch.complex64, device=field.device)
+    _call("lp_expand", field.device, _vp(field), n, _vp(out), int(n_out))
+    return out
+
+
+def coarse(field: torch.Tensor, order: int) -> torch.Tensor:
+    """order x order block mean (lp_coarse; beam2d.py:434-460)."""
+    n = _grid(field, "field")
+    if order < 1 or n % order:
+        raise ValueError(f"mean_order={order} must divide npoints={n}")
+    out = torch.empty((n // order, n // order), dtype=torch.complex64, device=field.device)
+    _call("lp_coarse", field.device, _vp(field), n, _vp(out), int(order))
+    return out
+
+
+def crop(field: torch.Tensor, first: int, n_keep: int, x0: float, dL_in: float, n_out: int,
+         dL_out: float) -> torch.Tensor:
+    """Bilinear resampling of the window field[first:first+n_keep]^2 onto the
+    centred n_out grid of spacing dL_out (lp_crop; beam2d.py:406-432)."""
+    n = _grid(field, "field")
+    out = torch.empty((n_out, n_out), dtype=torch.complex64, device=field.device)
+    _call("lp_crop", field.device, _vp(field), n, int(first), int(n_keep), float(x0),
+          float(dL_in), _vp(out), int(n_out), float(dL_out))
     return out
 
 

@@ -47,6 +47,7 @@ import numpy as np
 import torch
 
 from . import backend as B
+from . import generators as G
 
 nm = 1e-7
 um = 1e-4
@@ -140,10 +141,12 @@ class Beam2D:
         self.dL = self.area_size / self.npoints
         self.X = np.arange(-self.npoints // 2, self.npoints // 2, 1) * self.dL
         self.Y = self.X.reshape((-1, 1))
+        self._X0 = self.X.copy()  # to detect in-place changes of X (see lens)
         self.k0 = 1 / self.wl
         self.Kx = np.fft.fftfreq(self.npoints, d=self.dL)
         self.Ky = self.Kx.reshape((-1, 1))
         self._Kz = None
+        self._xscale = 1.0  # factor lens_image leaves on X (beam2d.py:529-531)
 
     @property
     def Kz(self):
@@ -247,7 +250,16 @@ class Beam2D:
         """Thin lens exp(i*(X^2+Y^2)*k0/(2f)) (beam2d.py:492-511)."""
         if not (isinstance(f, (int, float, np.floating)) and math.isfinite(f) and f != 0):
             raise ValueError("focal length must be a finite non-zero number")
-        self._pend_invf += 1.0 / f
+        if not np.array_equal(self.X, self._X0 * self._xscale):
+            # The reference builds the phase from self.X, which profile
+            # generators shift in place (gaussian_beam's `x -= x0` on the grid
+            # and its Y view): centre the lens there, in FP64 on the device.
+            X = torch.as_tensor(self.X, dtype=torch.float64, device=self.device)
+            ph = torch.remainder((X[None, :] ** 2 + X[:, None] ** 2) * (self.k0 / (2 * f)),
+                                 2 * math.pi)
+            self.coordinate_filter(f_init=torch.polar(torch.ones_like(ph), ph).to(torch.complex64))
+            return
+        self._pend_invf += self._xscale ** 2 / f  # the phase follows the (scaled) grid X
         self._spec = None
         self._spec_dz = 0.0
 
@@ -269,7 +281,12 @@ class Beam2D:
                           fargs: tuple = ()) -> None:
         """field *= f_gen(X, Y, *fargs) * f_init; spectrum = fft2(field)
         (beam2d.py:310-342)."""
-        m = self._mask(f_init, f_gen, fargs, self.X, self.Y)
+        m = None
+        if f_init is None and f_gen is not None:
+            # deterministic generators become a 2N table evaluated in the pass
+            m = G.compact(f_gen, fargs, self.X, self.Y, self.device)
+        if m is None:
+            m = self._mask(f_init, f_gen, fargs, self.X, self.Y)
         if m is None:
             self._flush_x()
             self._spec = None
@@ -284,7 +301,11 @@ class Beam2D:
                         fargs: tuple = ()) -> None:
         """spectrum *= f_gen(Kx, Ky, *fargs) * f_init; field = ifft2(spectrum)
         (beam2d.py:344-373)."""
-        m = self._mask(f_init, f_gen, fargs, self.Kx, self.Ky)
+        m = None
+        if f_init is None and f_gen is not None:
+            m = G.compact(f_gen, fargs, self.Kx, self.Ky, self.device, allow_span=False)
+        if m is None:
+            m = self._mask(f_init, f_gen, fargs, self.Kx, self.Ky)
         if self._spec is None:
             spec = torch.empty_like(self._field)
             lens_f = (1.0 / self._pend_invf) if self._pend_invf != 0.0 else 0.0
@@ -314,47 +335,124 @@ class Beam2D:
         """angle(field) (beam2d.py:723-738); numpy when numpy_output."""
         return self._np(torch.angle(self.field))
 
+    def _moments(self):
+        """(m0, m1, m2, m3, m4) of lp_beam_moments on the host; the reference's
+        np.average raises ZeroDivisionError for a zero field, so does this."""
+        m = B.beam_moments(self.field).cpu().tolist()
+        if not m[0] > 0:
+            raise ZeroDivisionError("Weights sum to zero, can't be normalized")
+        return m
+
     @property
     def centroid(self):
         """Intensity-weighted centre (Xc, Yc, nxc, nyc) (beam2d.py:669-685)."""
         n = self.npoints // 2
-        I = B.iprofile(self.field).double()
-        c = (torch.arange(-n, n, device=self.device, dtype=torch.float64) * self.dL)
-        tot = I.sum()
-        Xc = float((I.sum(0) * c).sum() / tot)
-        Yc = float((I.sum(1) * c).sum() / tot)
+        m = self._moments()
+        Xc = self.dL * (m[1] / m[0])
+        Yc = self.dL * (m[2] / m[0])
         return Xc, Yc, int(Xc / self.dL) + n, int(Yc / self.dL) + n
 
     @property
     def D4sigma(self):
         """Beam widths 4*sigma along x and y (beam2d.py:687-704)."""
-        n = self.npoints // 2
-        I = B.iprofile(self.field).double()
-        c = (torch.arange(-n, n, device=self.device, dtype=torch.float64) * self.dL)
-        Xc, Yc, _, _ = self.centroid
-        tot = I.sum()
-        sx = math.sqrt(float((I.sum(0) * (c - Xc) ** 2).sum() / tot))
-        sy = math.sqrt(float((I.sum(1) * (c - Yc) ** 2).sum() / tot))
-        return 4 * sx, 4 * sy
+        m = self._moments()
+        return 4 * self.dL * math.sqrt(m[3] / m[0]), 4 * self.dL * math.sqrt(m[4] / m[0])
 
     @property
     def centroid_intensity(self) -> float:
         """Intensity at the centroid pixel (beam2d.py:740-752)."""
         _, _, nxc, nyc = self.centroid
-        return float(B.iprofile(self.field)[nyc, nxc])
+        v = self.field[nyc, nxc]
+        return float(v.real ** 2 + v.imag ** 2)
 
-    # ---------------------------------------------- outside this backend --
+    # --------------------------------------------------- grid management --
+    def _regrid(self, field):
+        """Swap in a field on the new grid; the spectrum is fft2(field), made
+        when read (the reference computes it eagerly)."""
+        self._field = field
+        self._pend_invf = 0.0
+        self._pend_xmask = None
+        self._spec = None
+        self._spec_dz = 0.0
+
+    def _check_new_n(self, n, what):
+        if not B.is_supported(n):
+            raise ValueError(f"{what}: npoints={n} is not supported by the GB300 backend "
+                             "(powers of two from 16 to 4096)")
+
     def expand(self, area_size: float):
-        raise NotImplementedError("Beam2D.expand is not provided by the GB300 propagation backend")
+        """Grow the area to ``area_size`` at constant dL, padding every side
+        with copies of the edge values (beam2d.py:375-404)."""
+        old = self.npoints
+        n = int(self.npoints * area_size / self.area_size)
+        n -= n % 2
+        if n < old:
+            raise ValueError("expand: the new area must not be smaller than the current one")
+        self._check_new_n(n, "expand")
+        f = B.expand(self.field, n)
+        self.npoints = n
+        self.area_size = area_size
+        self._construct_grids()
+        self._regrid(f)
 
     def crop(self, area_size: float, npoints: int = 0):
-        raise NotImplementedError("Beam2D.crop is not provided by the GB300 propagation backend")
+        """Resample the central window |X| < area_size/2 onto a grid of
+        ``area_size`` and ``npoints`` points (the current count if 0) by
+        bilinear interpolation, as the reference's ``interp2d`` does
+        (beam2d.py:406-432)."""
+        nc = self.npoints // 2
+        n = int(np.count_nonzero(np.abs(self.X) < area_size / 2)) // 2
+        if n < 1:
+            raise ValueError("crop: the window holds no grid points")
+        first = nc - n
+        x0, dL_in = float(self.X[first]), self.dL
+        new_n = npoints if npoints else self.npoints
+        self._check_new_n(new_n, "crop")
+        f = self.field
+        self.npoints = new_n
+        self.area_size = area_size
+        self._construct_grids()
+        self._regrid(B.crop(f, first, 2 * n, x0, dL_in, new_n, self.dL))
 
     def coarse(self, mean_order: int = 1):
-        raise NotImplementedError("Beam2D.coarse is not provided by the GB300 propagation backend")
+        """Divide npoints by ``mean_order`` with a block mean of the field
+        (beam2d.py:434-460)."""
+        if mean_order < 1 or self.npoints % mean_order:
+            raise ValueError(f"coarse: mean_order={mean_order} must divide npoints={self.npoints}")
+        n = self.npoints // mean_order
+        self._check_new_n(n, "coarse")
+        f = B.coarse(self.field, mean_order)
+        self.npoints = n
+        self._construct_grids()
+        self._regrid(f)
 
+    # ---------------------------------------------- outside this backend --
     def lens_image(self, f: float, l1: float, l2: float):
-        raise NotImplementedError("Beam2D.lens_image is not provided by the GB300 propagation backend")
+        """Image through a lens between conjugate planes (beam2d.py:513-537):
+        field = s * field(s*X, s*Y) * exp(-i*(X^2+Y^2)*k0*(l1+l2)/(2*l2^2)),
+        s = -l1/l2, resampled bilinearly like the reference's interp2d.  As
+        there, the sample coordinates are sorted before evaluation (so a
+        negative s does not mirror the image), and the grid X (and its view
+        Y) is left scaled by s; later lenses follow that scaled grid."""
+        if not (l2 != 0 and math.isfinite(l1) and math.isfinite(l2)):
+            raise ValueError("lens_image: l1, l2 finite and l2 non-zero")
+        if self._xscale < 0:
+            raise NotImplementedError("lens_image on a grid mirrored by a previous lens_image")
+        s = -l1 / l2
+        if s == 0:
+            raise ValueError("lens_image: l1 must be non-zero")
+        n = self.npoints
+        dL_in = float(self.X[1] - self.X[0])
+        x0 = float(self.X[0]) - (abs(s) * dL_in if s < 0 else 0.0)
+        g = B.crop(self.field, 0, n, x0, dL_in, n, abs(s) * dL_in)
+        g *= s
+        self._regrid(g)
+        # phase = -(X^2+Y^2)*k0*(l1+l2)/(2*l2^2): a lens of focal length
+        # -l2^2/(l1+l2) on the current grid
+        if l1 + l2 != 0:
+            self.lens(-l2 ** 2 / (l1 + l2))
+        self.X *= s
+        self._xscale *= s
 
     def deconstruct_by_modes(self, *a, **k):
         raise NotImplementedError("mode decomposition is not provided by the GB300 propagation backend")

@@ -167,9 +167,11 @@ lp_status check_ptr(const void* p, const char* name, bool required) {
   return LP_OK;
 }
 
-lp_status check_mask(const void* m, int type, const char* name) {
-  if (type < LP_MASK_NONE || type > LP_MASK_C128)
+lp_status check_mask(const void* m, int type, const char* name, bool k_domain = false) {
+  if (type < LP_MASK_NONE || type > LP_MASK_SPAN_I32)
     return fail(LP_ERR_INVALID_ARGUMENT, "%s: unknown mask type %d", name, type);
+  if (k_domain && type == LP_MASK_SPAN_I32)
+    return fail(LP_ERR_INVALID_ARGUMENT, "%s: LP_MASK_SPAN_I32 is an x-domain mask type", name);
   if (type == LP_MASK_NONE) return LP_OK;
   if (!m) return fail(LP_ERR_INVALID_ARGUMENT, "%s: NULL with mask type %d", name, type);
   const uintptr_t a = reinterpret_cast<uintptr_t>(m);
@@ -254,7 +256,7 @@ __global__ void xmul_kernel(float2* __restrict__ f, int n, RowOps ops) {
       const float jx = (float)(x - n / 2), jy = (float)(y - n / 2);
       m = cis_cycles(lens_cycles(ops.kap_hi, ops.kap_lo, fmaf(jx, jx, jy * jy)), 1.0f);
     }
-    if (ops.xmask) m = cmul(m, mask_value(ops.xmask, ops.xmask_type, i));
+    if (ops.xmask) m = cmul(m, mask_value_xy(ops.xmask, ops.xmask_type, y, x, n));
     if (ops.conj) m = cconj(m);
     f[i] = cmul(f[i], m);
   }
@@ -446,7 +448,7 @@ lp_status lp_propagate(lp_cfloat* spectrum, lp_cfloat* field, int n, double area
   LP_TRY(check_grid(n));
   LP_TRY(check_ptr(spectrum, "spectrum", true));
   LP_TRY(check_ptr(field, "field", true));
-  LP_TRY(check_mask(kmask, kmask_type, "kmask"));
+  LP_TRY(check_mask(kmask, kmask_type, "kmask", true));
   LP_TRY(check_geometry(area_size, wl));
   if (!std::isfinite(z)) return fail(LP_ERR_INVALID_ARGUMENT, "z must be finite");
   if ((const void*)spectrum == (const void*)field)
@@ -482,7 +484,7 @@ lp_status lp_propagate_field(const lp_cfloat* field_in, lp_cfloat* field_out,
   if (iprofile_out && (reinterpret_cast<uintptr_t>(iprofile_out) & 3u))
     return fail(LP_ERR_MISALIGNED, "iprofile_out is not 4-byte aligned");
   LP_TRY(check_mask(xmask, xmask_type, "xmask"));
-  LP_TRY(check_mask(kmask, kmask_type, "kmask"));
+  LP_TRY(check_mask(kmask, kmask_type, "kmask", true));
   LP_TRY(check_geometry(area_size, wl));
   if (!std::isfinite(z) || !std::isfinite(lens_f))
     return fail(LP_ERR_INVALID_ARGUMENT, "z and lens_f must be finite");

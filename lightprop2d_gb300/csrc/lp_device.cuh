@@ -347,4 +347,18 @@ __device__ __forceinline__ float2 mask_value(const void* mask, int type, size_t 
   }
 }
 
+// Multiplier at row y, column x of an N x N mask of any type, including the
+// compact generator tables (7: separable fx[x]*fy[y], 8: per-column row span).
+__device__ __forceinline__ float2 mask_value_xy(const void* mask, int type, int y, int x, int n) {
+  if (type == 7) {
+    const float* t = reinterpret_cast<const float*>(mask);
+    return make_float2(__ldg(t + x) * __ldg(t + n + y), 0.0f);
+  }
+  if (type == 8) {
+    const int* t = reinterpret_cast<const int*>(mask);
+    return make_float2((y >= __ldg(t + x) && y < __ldg(t + n + x)) ? 1.0f : 0.0f, 0.0f);
+  }
+  return mask_value(mask, type, (size_t)y * n + x);
+}
+
 }  // namespace lp

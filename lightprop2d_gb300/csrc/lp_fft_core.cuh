@@ -201,7 +201,7 @@ __device__ __forceinline__ float2 xop_value(int y, int x, const RowOps& ops) {
     const float jx = (float)(x - N / 2), jy = (float)(y - N / 2);
     m = cis_cycles(lens_cycles(ops.kap_hi, ops.kap_lo, fmaf(jx, jx, jy * jy)), 1.0f);
   }
-  if (ops.xmask) m = cmul(m, mask_value(ops.xmask, ops.xmask_type, (size_t)y * N + x));
+  if (ops.xmask) m = cmul(m, mask_value_xy(ops.xmask, ops.xmask_type, y, x, N));
   if (ops.conj) m = cconj(m);
   return m;
 }
@@ -322,7 +322,7 @@ __device__ __forceinline__ void apply_spectral(float2 (&v)[16], float2* tab, int
       m = tab[a * C + c];
     }
     if (ops.kmask) {
-      float2 km = mask_value(ops.kmask, ops.kmask_type, (size_t)ky * N + kx);
+      float2 km = mask_value_xy(ops.kmask, ops.kmask_type, ky, kx, N);
       if (ops.conj) km = cconj(km);
       m = cmul(m, km);
     }

@@ -1,0 +1,131 @@
+// Intensity moments of a field for Beam2D.centroid / D4sigma /
+// centroid_intensity (beam2d.py:669-752): two read-only passes over the grid.
+//
+//   pass 1:  m0 = sum I,  m1 = sum jx*I,  m2 = sum jy*I
+//   pass 2:  m3 = sum (jx - xc)^2 I,  m4 = sum (jy - yc)^2 I,
+//            xc = m1/m0, yc = m2/m0 read from pass 1's result on the device
+//
+// with I = |field|^2 and jx = ix - n/2, jy = iy - n/2 (grid-index offsets
+// from the centre; the caller scales by dL).  The second moments are taken
+// about the centroid, as the reference does, so an off-centre beam loses no
+// precision to cancellation.  Each thread accumulates in FP32 over a strided
+// share of the grid (a few hundred points at most), then warps and CTAs
+// reduce in FP64 and one atomicAdd per CTA lands in the 5-double result.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "lightprop2d_gb300.h"
+#include "lp_internal.h"
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Adds v[0..K) over the CTA into out[0..K) (one atomicAdd per value per CTA).
+template <int K>
+__device__ __forceinline__ void cta_add(const float (&v)[K], double* out) {
+  __shared__ double part[K][kThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const double s = warp_sum((double)v[k]);
+    if (lane == 0) part[k][w] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      double s = threadIdx.x < kThreads / 32 ? part[k][threadIdx.x] : 0.0;
+      s = warp_sum(s);
+      if (threadIdx.x == 0) atomicAdd(out + k, s);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) moments1_kernel(const float2* __restrict__ f,
+                                                            int logn, double* out) {
+  const int n = 1 << logn, h = n >> 1;
+  const size_t n2 = (size_t)n * n;
+  float s[3] = {0.0f, 0.0f, 0.0f};
+  for (size_t i = blockIdx.x * (size_t)kThreads + threadIdx.x; i < n2;
+       i += (size_t)gridDim.x * kThreads) {
+    const float2 v = f[i];
+    const float I = fmaf(v.x, v.x, v.y * v.y);
+    const float jx = (float)((int)(i & (size_t)(n - 1)) - h);
+    const float jy = (float)((int)(i >> logn) - h);
+    s[0] += I;
+    s[1] = fmaf(jx, I, s[1]);
+    s[2] = fmaf(jy, I, s[2]);
+  }
+  cta_add<3>(s, out);
+}
+
+__global__ void __launch_bounds__(kThreads) moments2_kernel(const float2* __restrict__ f,
+                                                            int logn, double* out) {
+  const int n = 1 << logn, h = n >> 1;
+  const size_t n2 = (size_t)n * n;
+  const double m0 = out[0];
+  const float xc = m0 > 0.0 ? (float)(out[1] / m0) : 0.0f;
+  const float yc = m0 > 0.0 ? (float)(out[2] / m0) : 0.0f;
+  float s[2] = {0.0f, 0.0f};
+  for (size_t i = blockIdx.x * (size_t)kThreads + threadIdx.x; i < n2;
+       i += (size_t)gridDim.x * kThreads) {
+    const float2 v = f[i];
+    const float I = fmaf(v.x, v.x, v.y * v.y);
+    const float dx = (float)((int)(i & (size_t)(n - 1)) - h) - xc;
+    const float dy = (float)((int)(i >> logn) - h) - yc;
+    s[0] = fmaf(dx * dx, I, s[0]);
+    s[1] = fmaf(dy * dy, I, s[1]);
+  }
+  cta_add<2>(s, out + 3);
+}
+
+int g_sms_metrics = 0;
+
+}  // namespace
+
+extern "C" lp_status lp_beam_moments(const lp_cfloat* field, int n, double* moments,
+                                     void* stream) {
+  using namespace lp;
+  if (!lp_is_supported_n(n))
+    return (lp_status)set_last_error(LP_ERR_UNSUPPORTED_SIZE,
+                                     "lp_beam_moments: npoints must be a power of two in 16..4096");
+  if (!field || !moments)
+    return (lp_status)set_last_error(LP_ERR_INVALID_ARGUMENT, "lp_beam_moments: NULL pointer");
+  if ((reinterpret_cast<uintptr_t>(field) & 7u) || (reinterpret_cast<uintptr_t>(moments) & 7u))
+    return (lp_status)set_last_error(LP_ERR_MISALIGNED, "lp_beam_moments: 8-byte alignment");
+  if (!g_sms_metrics) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sms_metrics, cudaDevAttrMultiProcessorCount, dev);
+    if (g_sms_metrics <= 0) g_sms_metrics = 1;
+  }
+  int logn = 0;
+  while ((1 << logn) < n) ++logn;
+  const size_t n2 = (size_t)n * n;
+  const size_t want = (n2 + kThreads * 16 - 1) / (kThreads * 16);  // >= 16 points a thread
+  const int grid = (int)(want < (size_t)g_sms_metrics * 4 ? (want ? want : 1)
+                                                          : (size_t)g_sms_metrics * 4);
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaMemsetAsync(moments, 0, 5 * sizeof(double), st);
+  if (e == cudaSuccess) {
+    moments1_kernel<<<grid, kThreads, 0, st>>>(reinterpret_cast<const float2*>(field), logn,
+                                               moments);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) {
+    moments2_kernel<<<grid, kThreads, 0, st>>>(reinterpret_cast<const float2*>(field), logn,
+                                               moments);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess)
+    return (lp_status)set_last_error(LP_ERR_CUDA, cudaGetErrorString(e));
+  return LP_OK;
+}

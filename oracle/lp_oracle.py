@@ -195,3 +195,85 @@ def gaussian(npoints, area_size, A0, rho0):
     """profiles.gaussian_beam (profiles.py:64-71) on the Beam2D grid."""
     g = grids(area_size, npoints, 1.0)
     return A0 * np.exp(-(g["X"] ** 2 + g["Y"] ** 2) / rho0 ** 2)
+
+
+# --------------------------------------------------------------------------
+# Beam metrics and grid management (beam2d.py:375-460, :669-752).
+# --------------------------------------------------------------------------
+
+def centroid(field, dL):
+    """``Beam2D.centroid`` (beam2d.py:669-685): (Xc, Yc, nxc, nyc)."""
+    n = field.shape[0] // 2
+    Y, X = np.mgrid[-n:n, -n:n] * dL
+    I = np.abs(field) ** 2
+    Xc = np.average(X, weights=I)
+    Yc = np.average(Y, weights=I)
+    return Xc, Yc, int(Xc / dL) + n, int(Yc / dL) + n
+
+
+def d4sigma(field, dL):
+    """``Beam2D.D4sigma`` (beam2d.py:687-704): 4*sigma along x and y."""
+    n = field.shape[0] // 2
+    I = np.abs(field) ** 2
+    Y, X = np.mgrid[-n:n, -n:n] * dL
+    Xc, Yc, _, _ = centroid(field, dL)
+    return (4 * np.sqrt(np.average((X - Xc) ** 2, weights=I)),
+            4 * np.sqrt(np.average((Y - Yc) ** 2, weights=I)))
+
+
+def centroid_intensity(field, dL):
+    """``Beam2D.centroid_intensity`` (beam2d.py:740-752)."""
+    _, _, nxc, nyc = centroid(field, dL)
+    return float(np.abs(field[nyc, nxc]) ** 2)
+
+
+def expand(field, n_out):
+    """``Beam2D.expand`` field step (beam2d.py:390-402): pad (n_out - n)/2
+    points on every side with copies of the edge rows/columns."""
+    d = (n_out - field.shape[0]) // 2
+    return np.pad(field, d, mode="edge")
+
+
+def coarse(field, order):
+    """``Beam2D.coarse`` field step (beam2d.py:455-459): block mean."""
+    n = field.shape[0] // order
+    return field.reshape((n, order, n, order)).mean((1, 3))
+
+
+def bilinear_nearest(grid_x, values, qx):
+    """2-D linear interpolation of ``values`` (rows and columns on the
+    ascending axis ``grid_x``) at the ascending query axis ``qx`` for both
+    dimensions, nearest value outside the axis range.  This is what the
+    reference's ``scipy.interpolate.interp2d(x, x, z)`` (kind="linear",
+    fill_value=None) returns on a rectangular grid; interp2d itself was
+    removed from SciPy 1.14, so it is restated here."""
+    qx = np.sort(np.asarray(qx, dtype=np.float64))
+    p = np.interp(qx, grid_x, np.arange(len(grid_x), dtype=np.float64))
+    i0 = np.clip(np.floor(p).astype(int), 0, len(grid_x) - 1)
+    i1 = np.minimum(i0 + 1, len(grid_x) - 1)
+    w = p - i0
+    v = np.asarray(values)
+    rows = v[i0, :] * (1 - w)[:, None] + v[i1, :] * w[:, None]
+    return rows[:, i0] * (1 - w)[None, :] + rows[:, i1] * w[None, :]
+
+
+def crop(field, X, area_size, npoints_out, area_out):
+    """``Beam2D.crop`` field step (beam2d.py:417-430): the central window
+    |X| < area_size/2 resampled onto the new centred grid."""
+    nc = field.shape[0] // 2
+    n = len(X[np.abs(X) < area_size / 2]) // 2
+    old_x = X[nc - n:nc + n]
+    win = field[nc - n:nc + n, nc - n:nc + n]
+    new_x = np.arange(-npoints_out // 2, npoints_out // 2, 1) * (area_out / npoints_out)
+    return bilinear_nearest(old_x, win, new_x)
+
+
+def lens_image(field, X, k0, l1, l2):
+    """``Beam2D.lens_image`` field step (beam2d.py:524-535): the field
+    resampled at the sorted coordinates s*X (s = -l1/l2), times s and the
+    phase -(X^2+Y^2)*k0*(l1+l2)/(2*l2^2)."""
+    s = -l1 / l2
+    Y = X.reshape((-1, 1))
+    phase = -(X ** 2 + Y ** 2) * k0 * (l1 + l2) / 2 / l2 ** 2
+    g = bilinear_nearest(X, field, X * s)
+    return s * g * (np.cos(phase) + 1j * np.sin(phase))

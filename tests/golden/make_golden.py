@@ -180,6 +180,42 @@ def main(ref_path):
         out[f"kat_{tag}_I"] = np.array(vals)
         out[f"kat_{tag}_k0"] = np.array(K.k0)
 
+    # --- beam metrics (beam2d.py:669-752): centroid, D4sigma, centroid_intensity.
+    def metrics(beam):
+        Xc, Yc, nxc, nyc = beam.centroid
+        dx, dy = beam.D4sigma
+        return np.array([Xc, Yc, nxc, nyc, dx, dy, beam.centroid_intensity])
+
+    out["met_cfg1"] = metrics(b)
+    M = lp.Beam2D(1 * mm, 512, 632 * nm, init_field_gen=lp.gaussian_beam,
+                  init_gen_args=(1, 50 * um, 200 * um, -150 * um), complex_bits=64)
+    out["met_off_in"] = metrics(M)
+    M.lens(3.0)
+    M.propagate(2.0)
+    out["met_off_prop"] = metrics(M)
+
+    # --- grid management (beam2d.py:375-460): expand (edge replication) and
+    #     coarse (block mean); each ends with a new FFT.  crop needs
+    #     scipy.interpolate.interp2d, removed from SciPy >= 1.14.
+    G = lp.Beam2D(1 * mm, 128, 632 * nm, init_field_gen=lp.gaussian_beam,
+                  init_gen_args=(1, 150 * um, 100 * um, 0), complex_bits=64)
+    G.propagate(1.0)
+    out["grid_in"] = G.field.copy()
+    G.expand(2 * mm)
+    out["grid_expand_n"] = np.array(G.npoints)
+    out["grid_expand_field"] = G.field.copy()
+    out["grid_expand_spectrum"] = G.spectrum.copy()
+    G.coarse(2)
+    out["grid_coarse_n"] = np.array(G.npoints)
+    out["grid_coarse_field"] = G.field.copy()
+    out["grid_coarse_spectrum"] = G.spectrum.copy()
+    try:
+        G.crop(0.5 * mm)
+        out["grid_crop_runs"] = np.array(True)
+    except Exception as e:  # interp2d is gone from current SciPy
+        out["grid_crop_runs"] = np.array(False)
+        out["grid_crop_error"] = np.array(type(e).__name__)
+
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     print("wrote", len(out), "arrays")
 

@@ -115,3 +115,30 @@ def test_gaussian_known_answer(golden, tag):
         vals.append(b.iprofile[256, 256])
         b.propagate(0.02)
     assert np.allclose(vals, golden[f"kat_{tag}_I"], rtol=1e-12)
+
+
+def test_metrics_and_grid_oracle_match_reference(golden):
+    """Oracle restatements of centroid / D4sigma / centroid_intensity
+    (beam2d.py:669-752), expand and coarse (beam2d.py:375-460) reproduce the
+    reference's own outputs; crop's interp2d (gone from SciPy >= 1.14, the
+    reference raises there) is checked against SciPy's linear
+    RegularGridInterpolator with nearest-value clamping."""
+    b = golden["cfg1_field"]
+    dL = O.um * 200 / 256
+    m = [*O.centroid(b, dL), *O.d4sigma(b, dL), O.centroid_intensity(b, dL)]
+    assert np.allclose(m, golden["met_cfg1"], rtol=1e-12, atol=0)
+    assert np.array_equal(O.expand(golden["grid_in"], int(golden["grid_expand_n"])),
+                          golden["grid_expand_field"])
+    c = O.coarse(golden["grid_expand_field"], 2)
+    assert np.allclose(c, golden["grid_coarse_field"], rtol=1e-6, atol=1e-7)
+    assert not bool(golden["grid_crop_runs"])
+    from scipy.interpolate import RegularGridInterpolator
+    X = np.arange(-64, 64) * (0.1 / 128)
+    f = golden["grid_in"]
+    keep = X[np.abs(X) < 0.025]
+    nc, n = 64, len(keep) // 2
+    ox, win = X[nc - n:nc + n], f[nc - n:nc + n, nc - n:nc + n]
+    qx = np.arange(-40, 40) * (0.06 / 80)
+    q = np.clip(qx, ox[0], ox[-1])
+    ref = RegularGridInterpolator((ox, ox), win)(np.stack(np.meshgrid(q, q, indexing="ij"), -1))
+    assert np.allclose(O.crop(f, X, 0.05, 80, 0.06), ref, rtol=1e-12, atol=1e-15)

@@ -74,3 +74,77 @@ def test_torch_inputs():
     assert np.array_equal(P.round_hole(xt, yt, 8e-4).numpy(), P.round_hole(x, y, 8e-4))
     assert np.array_equal(P.square_slits(xt, yt, 4e-4, 1e-3).numpy(),
                           P.square_slits(x, y, 4e-4, 1e-3))
+
+
+# ---------------------------------------------------------------------------
+# Compact (2N-table) forms of the deterministic generators, which the first
+# FFT pass evaluates on the device (lightprop2d_gb300.generators).
+# ---------------------------------------------------------------------------
+def _dense(f_gen, fargs, x, y):
+    from lightprop2d_gb300 import generators as G
+    gm = G.compact(f_gen, fargs, x, y, "cpu")
+    assert gm is not None
+    return G.dense(gm, x.size).numpy()
+
+
+def _grid(n, dL):
+    x = np.arange(-n // 2, n // 2, 1) * dL
+    return x, x.reshape((-1, 1))
+
+
+def test_compact_generators_match_reference_golden(golden):
+    n, dL = 32, 1e-4
+    cases = [(P.plane_wave, (), "prof_plane"),
+             (P.round_hole, (8 * dL, 2 * dL, 0), "prof_round"),
+             (P.rectangle_hole, (10 * dL, 6 * dL, dL, 0), "prof_rect"),
+             (P.square_hole, (8 * dL,), "prof_square"),
+             (P.square_slits, (4 * dL, 10 * dL), "prof_slits")]
+    for f, args, key in cases:
+        x, y = _grid(n, dL)
+        assert np.array_equal(_dense(f, args, x, y), golden[key].astype(np.float32)), key
+    x, y = _grid(n, dL)
+    g = _dense(P.gaussian_beam, (1.5, 8 * dL, dL, -2 * dL), x.copy(), y.copy())  # as generated
+    assert np.allclose(g, golden["prof_gauss"], rtol=2e-7, atol=1e-12)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_compact_generators_match_dense_random(seed):
+    rng = np.random.default_rng(seed)
+    n = int(rng.choice([64, 256, 1024]))
+    dL = float(rng.uniform(0.5, 3)) * 1e-4
+    A = n * dL
+    R = float(rng.uniform(0.02, 0.4)) * A
+    x0, y0 = (float(v) for v in rng.uniform(-0.2, 0.2, 2) * A)
+    if seed % 2:  # grid-aligned parameters put points exactly on edges
+        R, x0, y0 = 12 * dL, 3 * dL, -5 * dL
+    for f, args in [(P.round_hole, (R, x0, y0)), (P.rectangle_hole, (R, 0.7 * R, x0, y0)),
+                    (P.square_hole, (R, x0, y0)), (P.square_slits, (0.3 * R, R, x0, y0)),
+                    (P.plane_wave, ())]:
+        x, y = _grid(n, dL)
+        ref = f(x.copy(), y.copy().reshape((-1, 1)), *args)
+        ref = np.broadcast_to(ref, (n, n)).astype(np.float32)
+        assert np.array_equal(_dense(f, args, x, y), ref), (f.__name__, n)
+    # gaussian_beam: values to FP32 rounding, and the in-place grid shift
+    x, y = _grid(n, dL)
+    xr = x.copy()
+    yr = xr.reshape((-1, 1))
+    ref = P.gaussian_beam(xr, yr, 2.0, R, x0, y0)
+    g = _dense(P.gaussian_beam, (2.0, R, x0, y0), x, y)
+    assert np.allclose(g, ref, rtol=3e-7, atol=1e-30)
+    assert np.array_equal(x, xr)
+
+
+def test_compact_generators_on_fftfreq_grid():
+    """Spectral masks: separable generators on the unshifted K grid."""
+    n, dL = 128, 1e-4
+    kx = np.fft.fftfreq(n, d=dL)
+    ky = kx.reshape((-1, 1))
+    for f, args in [(P.rectangle_hole, (800.0, 500.0)), (P.square_slits, (200.0, 900.0)),
+                    (P.gaussian_beam, (1.0, 700.0))]:
+        ref = f(kx.copy(), kx.copy().reshape((-1, 1)), *args)
+        ref = np.broadcast_to(ref, (n, n)).astype(np.float32)
+        got = _dense(f, args, kx.copy(), kx.copy().reshape((-1, 1)))
+        assert np.allclose(got, ref, rtol=3e-7, atol=1e-30), f.__name__
+    from lightprop2d_gb300 import generators as G
+    assert G.compact(P.round_hole, (500.0,), kx, ky, "cpu", allow_span=False) is None
+    assert G.compact(P.random_round_hole, (500.0,), kx, ky, "cpu") is None
