@@ -215,6 +215,21 @@ lp_status lp_coarse(const lp_cfloat* in, int n_in, lp_cfloat* out, int order, vo
 lp_status lp_crop(const lp_cfloat* in, int n_in, int first, int n_keep, double x0, double dL_in,
                   lp_cfloat* out, int n_out, double dL_out, void* stream);
 
+/* ------------------------------------------------------ mode decomposition --
+ * The mode basis is n_modes x nb^2 complex64 (row m = mode m, flattened
+ * row-major on an nb x nb grid), applied to the central nb x nb window of the
+ * n x n field ((n - nb)/2 points in from each edge).  HBM-bound
+ * matrix-vector products; coefficients are complex128 pairs in device memory. */
+/* Beam2D.deconstruct_by_modes(mode="scalar") (beam2d.py:574-600):
+ * coeffs[m] = sum_p modes[m][p] * window[p]  (no conjugation, as there). */
+lp_status lp_modes_project(const lp_cfloat* modes, int n_modes, int nb, const lp_cfloat* field,
+                           int n, double* coeffs, void* stream);
+/* Beam2D.construct_by_modes (beam2d.py:650-667): field = sum_m coeffs[m]*mode_m
+ * inside the window and 0 outside (the zero padding of _expand_basis,
+ * beam2d.py:539-559). */
+lp_status lp_modes_combine(const lp_cfloat* modes, int n_modes, int nb, const double* coeffs,
+                           lp_cfloat* field, int n, void* stream);
+
 /* ------------------------------------------------------------- batches --
  * Many beams of uneven grid sizes in ONE persistent launch.  Each beam runs
  * lens(lens_f) -> propagate(z) -> iprofile on its own grid, in place:

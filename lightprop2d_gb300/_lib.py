@@ -81,6 +81,8 @@ SIGNATURES = {
     "lp_expand": [_vp, _i, _vp, _i, _vp],
     "lp_coarse": [_vp, _i, _vp, _i, _vp],
     "lp_crop": [_vp, _i, _i, _i, _d, _d, _vp, _i, _d, _vp],
+    "lp_modes_project": [_vp, _i, _i, _vp, _i, _vp, _vp],
+    "lp_modes_combine": [_vp, _i, _i, _vp, _vp, _i, _vp],
     "lp_apply_transfer": [_vp, _i, _d, _d, _d, _u, _vp],
     "lp_plain_propagate_field": [_vp, _vp, _i, _d, _d, _d, _u, _vp],
     "lp_plain_propagate_field_noalloc": [_vp, _vp, _i, _d, _d, _d, _u, _vp],

@@ -48,6 +48,7 @@ import torch
 
 from . import backend as B
 from . import generators as G
+from . import modes as M
 
 nm = 1e-7
 um = 1e-4
@@ -454,11 +455,34 @@ class Beam2D:
         self.X *= s
         self._xscale *= s
 
-    def deconstruct_by_modes(self, *a, **k):
-        raise NotImplementedError("mode decomposition is not provided by the GB300 propagation backend")
+    # ------------------------------------------------- mode decomposition --
+    def _coeffs_out(self, c: torch.Tensor):
+        self.modes_coeffs = c.cpu().numpy() if self.numpy_output else c
+        return self.modes_coeffs
 
-    fast_deconstruct_by_modes = deconstruct_by_modes
-    construct_by_modes = deconstruct_by_modes
+    def deconstruct_by_modes(self, modes_list, mode: str = "scalar"):
+        """Mode coefficients of the central window of the field
+        (beam2d.py:561-600): ``scalar`` = modes @ window (lp_modes_project),
+        ``lstsq`` = least-squares solution.  ``modes_list`` may be a
+        ``ModeBasis`` (uploaded once) or a list / array of flattened modes."""
+        basis = M.ModeBasis(modes_list, self.device)
+        if mode == "scalar":
+            c = M.project(basis, self.field)
+        elif mode == "lstsq":
+            c = M.lstsq(basis, self.field)
+        else:
+            raise ValueError(f"unknown mode {mode!r}: 'scalar' or 'lstsq'")
+        return self._coeffs_out(c)
+
+    def fast_deconstruct_by_modes(self, modes_matrix_t, modes_matrix_dot_t):
+        """lstsq(modes_matrix_dot_t, modes_matrix_t . window) (beam2d.py:602-648)."""
+        return self._coeffs_out(M.fast_lstsq(modes_matrix_t, modes_matrix_dot_t, self.field))
+
+    def construct_by_modes(self, modes_list, modes_coeffs):
+        """field = sum_i c_i * mode_i, zero outside the modes' window; the
+        spectrum follows (beam2d.py:650-667)."""
+        basis = M.ModeBasis(modes_list, self.device)
+        self._regrid(M.combine(basis, modes_coeffs, self.npoints, self.device))
 
     def __repr__(self) -> str:
         return (f"Beam {self.npoints:d}x{self.npoints:d} points" +

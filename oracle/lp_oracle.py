@@ -277,3 +277,44 @@ def lens_image(field, X, k0, l1, l2):
     phase = -(X ** 2 + Y ** 2) * k0 * (l1 + l2) / 2 / l2 ** 2
     g = bilinear_nearest(X, field, X * s)
     return s * g * (np.cos(phase) + 1j * np.sin(phase))
+
+
+# --------------------------------------------------------------------------
+# Mode decomposition (beam2d.py:539-667).
+# --------------------------------------------------------------------------
+
+def _window(field, nb):
+    n = field.shape[0]
+    d = (n - nb) // 2
+    return field[d:n - d, d:n - d].flatten()
+
+
+def modes_scalar(field, modes):
+    """deconstruct_by_modes(mode="scalar") (beam2d.py:593-596): modes @ window."""
+    modes = np.asarray(modes)
+    nb = int(np.sqrt(modes.shape[1]))
+    return np.vstack(modes) @ _window(field, nb)
+
+
+def modes_lstsq(field, modes):
+    """deconstruct_by_modes(mode="lstsq") (beam2d.py:597-599)."""
+    modes = np.asarray(modes)
+    nb = int(np.sqrt(modes.shape[1]))
+    return np.linalg.lstsq(np.vstack(modes).T, _window(field, nb), rcond=-1)[0]
+
+
+def modes_fast(field, modes_matrix_t, modes_matrix_dot_t):
+    """fast_deconstruct_by_modes (beam2d.py:639-648)."""
+    nb = int(np.sqrt(modes_matrix_t.shape[1]))
+    return np.linalg.lstsq(modes_matrix_dot_t, modes_matrix_t.dot(_window(field, nb)),
+                           rcond=None)[0]
+
+
+def modes_combine(modes, coeffs, n):
+    """construct_by_modes with _expand_basis (beam2d.py:539-559, :662-666)."""
+    modes = np.asarray(modes)
+    nb = int(np.sqrt(modes.shape[1]))
+    d = (n - nb) // 2
+    out = np.zeros((n, n), dtype=np.complex128)
+    out[d:n - d, d:n - d] = np.einsum("ij,i->j", modes, coeffs).reshape(nb, nb)
+    return out

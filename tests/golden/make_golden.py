@@ -216,6 +216,32 @@ def main(ref_path):
         out["grid_crop_runs"] = np.array(False)
         out["grid_crop_error"] = np.array(type(e).__name__)
 
+    # --- mode decomposition (beam2d.py:539-667) with a synthetic complex
+    #     Hermite-Gauss-like basis on a 32x32 window of a 64x64 beam.
+    nb, w = 32, 6 * um
+    xb = (np.arange(nb) - nb / 2 + 0.5) * (1.5 * um)
+    XB, YB = np.meshgrid(xb, xb)
+    herm = [np.ones_like(xb), 2 * xb / w, 4 * (xb / w) ** 2 - 2, 8 * (xb / w) ** 3 - 12 * xb / w]
+    modes = []
+    for a_ in range(4):
+        for b_ in range(4 - a_):
+            mm = np.outer(herm[b_], herm[a_]) * np.exp(-(XB ** 2 + YB ** 2) / w ** 2)
+            mm = mm * np.exp(1j * 0.37 * (a_ + 2 * b_))
+            modes.append((mm / np.linalg.norm(mm)).ravel())
+    modes = np.array(modes)
+    Q = lp.Beam2D(96 * um, 64, 1064 * nm, init_field_gen=lp.gaussian_beam,
+                  init_gen_args=(1, 8 * um, 2 * um, -1 * um))
+    Q.propagate(50 * um)
+    out["modes_basis"] = modes
+    out["modes_field"] = Q.field.copy()
+    out["modes_scalar"] = Q.deconstruct_by_modes(modes)
+    out["modes_lstsq"] = Q.deconstruct_by_modes(modes, "lstsq")
+    mt = np.vstack(modes).T
+    out["modes_fast"] = Q.fast_deconstruct_by_modes(mt.T, mt.T.dot(mt))
+    Q.construct_by_modes(modes, out["modes_scalar"] * np.exp(0.5j))
+    out["modes_constructed"] = Q.field.copy()
+    out["modes_constructed_spectrum"] = Q.spectrum.copy()
+
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     print("wrote", len(out), "arrays")
 

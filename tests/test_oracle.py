@@ -142,3 +142,14 @@ def test_metrics_and_grid_oracle_match_reference(golden):
     q = np.clip(qx, ox[0], ox[-1])
     ref = RegularGridInterpolator((ox, ox), win)(np.stack(np.meshgrid(q, q, indexing="ij"), -1))
     assert np.allclose(O.crop(f, X, 0.05, 80, 0.06), ref, rtol=1e-12, atol=1e-15)
+
+
+def test_modes_oracle_matches_reference(golden):
+    f, m = golden["modes_field"], golden["modes_basis"]
+    assert np.allclose(O.modes_scalar(f, m), golden["modes_scalar"], rtol=1e-12, atol=0)
+    assert np.allclose(O.modes_lstsq(f, m), golden["modes_lstsq"], rtol=1e-9, atol=1e-12)
+    mt = np.vstack(m).T
+    assert np.allclose(O.modes_fast(f, mt.T, mt.T.dot(mt)), golden["modes_fast"], rtol=1e-9)
+    c = golden["modes_scalar"] * np.exp(0.5j)
+    assert np.allclose(O.modes_combine(m, c, 64), golden["modes_constructed"], rtol=1e-12,
+                       atol=1e-15)
