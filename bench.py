@@ -244,6 +244,79 @@ def batch_section(dev, stream, clocks, reps, check_oracle=True):
     }
 
 
+def next_rows_section(dev, stream, hbm):
+    """Per-op device time and effective HBM bandwidth (bytes each op must move
+    / time, against the measured copy peak) at 2048^2 unless stated."""
+    import torch
+    from lightprop2d_gb300 import backend as B
+    from lightprop2d_gb300 import generators as G
+    from lightprop2d_gb300 import modes as MD
+    from lightprop2d_gb300 import profiles as P
+
+    def t_us(fn, k=50):
+        """Device time per call: k calls captured in a CUDA graph and replayed,
+        so host-side call overhead is not timed."""
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(device=dev)
+        s.wait_stream(stream)
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                for _ in range(k):
+                    fn()
+        stream.wait_stream(s)
+        g.replay()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        g.replay()
+        b.record(stream)
+        torch.cuda.synchronize()
+        del g
+        return a.elapsed_time(b) / k * 1e3
+
+    def row(us, nbytes, note):
+        return {"us": round(us, 2), "bytes": int(nbytes),
+                "effective_gbs": round(nbytes / (us * 1e-6) / 1e9, 1),
+                "hbm_frac": round(nbytes / (us * 1e-6) / 1e9 / hbm, 3), "note": note}
+
+    n = 2048
+    f = torch.randn(n, n, dtype=torch.complex64, device=dev)
+    out = {}
+    mom = torch.empty(5, dtype=torch.float64, device=dev)
+    out["beam_moments"] = row(t_us(lambda: B.beam_moments(f, mom)), 2 * 8 * n * n,
+                              "two read passes (moments about the centroid)")
+    # coordinate_filter(f_gen=round_hole) folded into a propagate, vs a dense mask
+    X = np.arange(-n // 2, n // 2) * (0.2 / n)
+    gm = G.compact(P.round_hole, (0.05,), X.copy(), X.copy().reshape((-1, 1)), dev)
+    dense = torch.as_tensor(P.round_hole(X.copy(), X.copy().reshape((-1, 1)), 0.05), device=dev)
+    dense = dense.to(torch.uint8)
+    o = torch.empty_like(f)
+    tg = t_us(lambda: B.propagate_field(f, 0.2, WL, 1.0, out=o, xmask=gm))
+    td = t_us(lambda: B.propagate_field(f, 0.2, WL, 1.0, out=o, xmask=dense))
+    t0 = t_us(lambda: B.propagate_field(f, 0.2, WL, 1.0, out=o))
+    out["generator_in_pass"] = {"round_hole_table_us": round(tg, 2),
+                                "dense_u8_mask_us": round(td, 2), "no_mask_us": round(t0, 2),
+                                "note": "fused propagate with the aperture in the first pass"}
+    out["expand"] = row(t_us(lambda: B.expand(f, 2 * n), 20), 8 * n * n + 8 * 4 * n * n,
+                        "2048^2 -> 4096^2")
+    out["coarse"] = row(t_us(lambda: B.coarse(f, 2)), 8 * n * n + 8 * n * n // 4,
+                        "2048^2 -> 1024^2 block mean")
+    out["crop"] = row(t_us(lambda: B.crop(f, n // 4, n // 2, -0.05, 0.2 / n, n, 0.1 / n)),
+                      8 * n * n // 4 + 8 * n * n, "window 1024^2 resampled to 2048^2")
+    M, nb = 256, 1024
+    basis = MD.ModeBasis(torch.randn(M, nb * nb, dtype=torch.complex64, device=dev))
+    coef = torch.randn(M, dtype=torch.complex128, device=dev)
+    out["modes_project"] = row(t_us(lambda: MD.project(basis, f), 10), 8 * M * nb * nb,
+                               f"{M} modes x {nb}^2 window of a 2048^2 field")
+    out["modes_combine"] = row(t_us(lambda: MD.combine(basis, coef, n, f.device), 10),
+                               8 * M * nb * nb + 8 * n * n, f"{M} modes into a 2048^2 field")
+    del basis, f, o
+    return out
+
+
 # ----------------------------------------------------------------- GPU side --
 class ClockSampler:
     """nvidia-smi sampling of SM clocks and throttle reasons."""
@@ -578,6 +651,11 @@ def main():
 
         # Uneven batch: 4096 beams in one persistent launch (CUDA graph).
         extra["batch_uneven"] = batch_section(dev, stream, clocks, reps=20)
+        torch.cuda.empty_cache()
+
+        # Metrics, generators, grid management, mode decomposition.
+        with clocks.window():
+            extra["next_rows"] = next_rows_section(dev, stream, hbm)
         torch.cuda.empty_cache()
 
     # ----------------------------------------------------------------- e2e --

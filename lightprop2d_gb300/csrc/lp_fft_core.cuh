@@ -193,33 +193,96 @@ __device__ __forceinline__ void conj16(float2 (&v)[16]) {
 }
 
 // ------------------------------------------------------------------ rows --
-// x-domain multiplier (lens phase and/or mask) for row y at column x.
+// Multiply the thread's 16 points of row y (columns t + T*j) by an x-domain
+// mask.  The 16 loads are issued before any is used (independent requests
+// in flight); real masks ignore `conj`.
 template <int N>
-__device__ __forceinline__ float2 xop_value(int y, int x, const RowOps& ops) {
-  float2 m = make_float2(1.0f, 0.0f);
-  if (ops.lens) {
-    const float jx = (float)(x - N / 2), jy = (float)(y - N / 2);
-    m = cis_cycles(lens_cycles(ops.kap_hi, ops.kap_lo, fmaf(jx, jx, jy * jy)), 1.0f);
+__device__ __forceinline__ void apply_mask_row(float2 (&v)[16], const void* mask, int type,
+                                               int conj, int y, int t) {
+  constexpr int T = FftGeo<N>::T;
+  const size_t row = (size_t)y * N + t;
+  switch (type) {
+    case 1: {  // float32
+      const float* p = reinterpret_cast<const float*>(mask) + row;
+      float m[16];
+      static_for<16>([&](auto jc) { m[jc.value] = __ldg(p + T * jc.value); });
+      static_for<16>([&](auto jc) { v[jc.value] = cscale(v[jc.value], m[jc.value]); });
+      break;
+    }
+    case 3: {  // uint8 / bool
+      const uint8_t* p = reinterpret_cast<const uint8_t*>(mask) + row;
+      uint8_t m[16];
+      static_for<16>([&](auto jc) { m[jc.value] = __ldg(p + T * jc.value); });
+      static_for<16>([&](auto jc) { v[jc.value] = cscale(v[jc.value], (float)m[jc.value]); });
+      break;
+    }
+    case 2: {  // complex64
+      const float2* p = reinterpret_cast<const float2*>(mask) + row;
+      float2 m[16];
+      static_for<16>([&](auto jc) { m[jc.value] = __ldg(p + T * jc.value); });
+      static_for<16>([&](auto jc) {
+        v[jc.value] = cmul(v[jc.value], conj ? cconj(m[jc.value]) : m[jc.value]);
+      });
+      break;
+    }
+    case 7: {  // separable table: fx[x] * fy[y]
+      const float* fx = reinterpret_cast<const float*>(mask);
+      const float fy = __ldg(fx + N + y);
+      float m[16];
+      static_for<16>([&](auto jc) { m[jc.value] = __ldg(fx + t + T * jc.value); });
+      static_for<16>([&](auto jc) { v[jc.value] = cscale(v[jc.value], m[jc.value] * fy); });
+      break;
+    }
+    case 8: {  // per-column row span: lo[x] <= y < hi[x]
+      const int* lo = reinterpret_cast<const int*>(mask);
+      int a[16], b[16];
+      static_for<16>([&](auto jc) {
+        a[jc.value] = __ldg(lo + t + T * jc.value);
+        b[jc.value] = __ldg(lo + N + t + T * jc.value);
+      });
+      static_for<16>([&](auto jc) {
+        if (!(y >= a[jc.value] && y < b[jc.value])) v[jc.value] = make_float2(0.0f, 0.0f);
+      });
+      break;
+    }
+    default: {  // phase, float64, complex128: rolled
+#pragma unroll 1
+      for (int j = 0; j < 16; ++j) {
+        float2 m = mask_value_xy(mask, type, y, t + T * j, N);
+        if (conj) m = cconj(m);
+        // v[j] with a run-time j would spill the array: rotate instead
+        static_for<16>([&](auto jc) {
+          if (jc.value == j) v[jc.value] = cmul(v[jc.value], m);
+        });
+      }
+      break;
+    }
   }
-  if (ops.xmask) m = cmul(m, mask_value_xy(ops.xmask, ops.xmask_type, y, x, N));
-  if (ops.conj) m = cconj(m);
-  return m;
 }
 
-// Multiply the thread's 16 points of row y by the x-domain multiplier,
-// evaluated in a rolled loop into the thread's own buffer slots (one copy of
-// the phase code), then applied.  The slots must be free.
+// Multiply the thread's 16 points of row y by the x-domain multipliers: the
+// lens phase, evaluated in a rolled loop into the thread's own buffer slots
+// (one copy of the phase code), then the mask.  The slots must be free.
 template <int N, int SY = 1>
 __device__ __forceinline__ void apply_xops(float2 (&v)[16], float2* slots, int nthreads, int y,
                                            int t, const RowOps& ops) {
   constexpr int T = FftGeo<N>::T;
   const int tid = group_tid<SY>();
+  if (ops.lens) {
+    const float jy = (float)(y - N / 2);
 #pragma unroll 1
-  for (int j = 0; j < 16; ++j) slots[j * nthreads + tid] = xop_value<N>(y, t + T * j, ops);
-  static_for<16>([&](auto jc) {
-    constexpr int j = decltype(jc)::value;
-    v[j] = cmul(v[j], slots[j * nthreads + tid]);
-  });
+    for (int j = 0; j < 16; ++j) {
+      const float jx = (float)(t + T * j - N / 2);
+      float2 m = cis_cycles(lens_cycles(ops.kap_hi, ops.kap_lo, fmaf(jx, jx, jy * jy)), 1.0f);
+      if (ops.conj) m = cconj(m);
+      slots[j * nthreads + tid] = m;
+    }
+    static_for<16>([&](auto jc) {
+      constexpr int j = decltype(jc)::value;
+      v[j] = cmul(v[j], slots[j * nthreads + tid]);
+    });
+  }
+  if (ops.xmask) apply_mask_row<N>(v, ops.xmask, ops.xmask_type, ops.conj, y, t);
 }
 
 template <int N, bool CG = false>

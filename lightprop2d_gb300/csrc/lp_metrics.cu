@@ -21,6 +21,7 @@
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kUnroll = 4;  // loads in flight per thread
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -54,15 +55,24 @@ __global__ void __launch_bounds__(kThreads) moments1_kernel(const float2* __rest
   const int n = 1 << logn, h = n >> 1;
   const size_t n2 = (size_t)n * n;
   float s[3] = {0.0f, 0.0f, 0.0f};
-  for (size_t i = blockIdx.x * (size_t)kThreads + threadIdx.x; i < n2;
-       i += (size_t)gridDim.x * kThreads) {
-    const float2 v = f[i];
-    const float I = fmaf(v.x, v.x, v.y * v.y);
-    const float jx = (float)((int)(i & (size_t)(n - 1)) - h);
-    const float jy = (float)((int)(i >> logn) - h);
-    s[0] += I;
-    s[1] = fmaf(jx, I, s[1]);
-    s[2] = fmaf(jy, I, s[2]);
+  const size_t stride = (size_t)gridDim.x * kThreads;
+  for (size_t i0 = blockIdx.x * (size_t)kThreads + threadIdx.x; i0 < n2; i0 += kUnroll * stride) {
+    float2 v[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {  // independent loads in flight
+      const size_t i = i0 + u * stride;
+      v[u] = i < n2 ? __ldg(f + i) : make_float2(0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      const size_t i = i0 + u * stride;
+      const float I = fmaf(v[u].x, v[u].x, v[u].y * v[u].y);
+      const float jx = (float)((int)(i & (size_t)(n - 1)) - h);
+      const float jy = (float)((int)(i >> logn) - h);
+      s[0] += I;
+      s[1] = fmaf(jx, I, s[1]);
+      s[2] = fmaf(jy, I, s[2]);
+    }
   }
   cta_add<3>(s, out);
 }
@@ -75,14 +85,23 @@ __global__ void __launch_bounds__(kThreads) moments2_kernel(const float2* __rest
   const float xc = m0 > 0.0 ? (float)(out[1] / m0) : 0.0f;
   const float yc = m0 > 0.0 ? (float)(out[2] / m0) : 0.0f;
   float s[2] = {0.0f, 0.0f};
-  for (size_t i = blockIdx.x * (size_t)kThreads + threadIdx.x; i < n2;
-       i += (size_t)gridDim.x * kThreads) {
-    const float2 v = f[i];
-    const float I = fmaf(v.x, v.x, v.y * v.y);
-    const float dx = (float)((int)(i & (size_t)(n - 1)) - h) - xc;
-    const float dy = (float)((int)(i >> logn) - h) - yc;
-    s[0] = fmaf(dx * dx, I, s[0]);
-    s[1] = fmaf(dy * dy, I, s[1]);
+  const size_t stride = (size_t)gridDim.x * kThreads;
+  for (size_t i0 = blockIdx.x * (size_t)kThreads + threadIdx.x; i0 < n2; i0 += kUnroll * stride) {
+    float2 v[kUnroll];
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      const size_t i = i0 + u * stride;
+      v[u] = i < n2 ? __ldg(f + i) : make_float2(0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      const size_t i = i0 + u * stride;
+      const float I = fmaf(v[u].x, v[u].x, v[u].y * v[u].y);
+      const float dx = (float)((int)(i & (size_t)(n - 1)) - h) - xc;
+      const float dy = (float)((int)(i >> logn) - h) - yc;
+      s[0] = fmaf(dx * dx, I, s[0]);
+      s[1] = fmaf(dy * dy, I, s[1]);
+    }
   }
   cta_add<2>(s, out + 3);
 }

@@ -8,9 +8,10 @@
 //
 // Both are matrix-vector products over an M x P complex64 basis (P = nb^2):
 // HBM-bound (every basis element is read once, 8 B, for 8 flops), so they are
-// CUDA-core kernels reading the basis with coalesced 16-byte loads, not
-// tensor-core GEMMs.  Sums run in FP32 over runs of 16 terms and in FP64
-// across runs, so results carry FP32 rounding of the inputs only.
+// CUDA-core kernels reading the basis with coalesced loads, several in flight
+// per thread, not tensor-core GEMMs.  Sums run in FP32 over short runs (4
+// terms in the projection, 16 in the synthesis) and in FP64 across runs, so
+// results carry FP32 rounding of the inputs only.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -45,23 +46,33 @@ __global__ void __launch_bounds__(kThreads) project_kernel(const float2* __restr
   const long long p1 = p0 + kChunk < P ? p0 + kChunk : P;
   const float2* row = modes + (size_t)m * P;
   double ar = 0.0, ai = 0.0;
-  float fr = 0.0f, fi = 0.0f;
-  int k = 0;
-  for (long long p = p0 + threadIdx.x; p < p1; p += kThreads) {
-    const float2 a = __ldg(row + p);
-    const int r = (int)(p / nb), q = (int)(p - (long long)r * nb);
-    const float2 w = __ldg(field + (size_t)(first + r) * n + first + q);
-    fr = fmaf(a.x, w.x, fmaf(-a.y, w.y, fr));
-    fi = fmaf(a.x, w.y, fmaf(a.y, w.x, fi));
-    if (++k == 16) {
-      ar += fr;
-      ai += fi;
-      fr = fi = 0.0f;
-      k = 0;
+  // (r, q) of point p tracked incrementally (no division in the loop)
+  long long p = p0 + threadIdx.x;
+  int r = (int)(p / nb), q = (int)(p - (long long)r * nb);
+  while (p < p1) {
+    float fr = 0.0f, fi = 0.0f;
+    float2 a[4], w[4];
+    bool ok[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {  // four independent pairs of loads in flight
+      ok[u] = p < p1;
+      a[u] = ok[u] ? __ldg(row + p) : make_float2(0.0f, 0.0f);
+      w[u] = ok[u] ? __ldg(field + (size_t)(first + r) * n + first + q) : make_float2(0.0f, 0.0f);
+      p += kThreads;
+      q += kThreads;
+      while (q >= nb) {
+        q -= nb;
+        ++r;
+      }
     }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      fr = fmaf(a[u].x, w[u].x, fmaf(-a[u].y, w[u].y, fr));
+      fi = fmaf(a[u].x, w[u].y, fmaf(a[u].y, w[u].x, fi));
+    }
+    ar += fr;
+    ai += fi;
   }
-  ar += fr;
-  ai += fi;
   __shared__ double part[2][kThreads / 32];
   const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
   ar = warp_sum(ar);
