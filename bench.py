@@ -297,9 +297,14 @@ def next_rows_section(dev, stream, hbm):
     tg = t_us(lambda: B.propagate_field(f, 0.2, WL, 1.0, out=o, xmask=gm))
     td = t_us(lambda: B.propagate_field(f, 0.2, WL, 1.0, out=o, xmask=dense))
     t0 = t_us(lambda: B.propagate_field(f, 0.2, WL, 1.0, out=o))
+    ph = torch.rand(n, n, device=dev) * 6.283
+    tl = t_us(lambda: B.propagate_field(f, 0.2, WL, 1.0, out=o, lens_f=5.0))
+    tp = t_us(lambda: B.propagate_field(f, 0.2, WL, 1.0, out=o, xmask=ph, xmask_phase=True))
     out["generator_in_pass"] = {"round_hole_table_us": round(tg, 2),
-                                "dense_u8_mask_us": round(td, 2), "no_mask_us": round(t0, 2),
-                                "note": "fused propagate with the aperture in the first pass"}
+                                "dense_u8_mask_us": round(td, 2), "lens_us": round(tl, 2),
+                                "phase_mask_us": round(tp, 2), "no_mask_us": round(t0, 2),
+                                "note": "fused propagate with the multiplier in the first pass"}
+    del ph
     out["expand"] = row(t_us(lambda: B.expand(f, 2 * n), 20), 8 * n * n + 8 * 4 * n * n,
                         "2048^2 -> 4096^2")
     out["coarse"] = row(t_us(lambda: B.coarse(f, 2)), 8 * n * n + 8 * n * n // 4,

@@ -225,6 +225,17 @@ __device__ __forceinline__ void apply_mask_row(float2 (&v)[16], const void* mask
       });
       break;
     }
+    case 4: {  // float32 phase: exp(i*phi)
+      const float* p = reinterpret_cast<const float*>(mask) + row;
+      float ph[16];
+      static_for<16>([&](auto jc) { ph[jc.value] = __ldg(p + T * jc.value); });
+      static_for<16>([&](auto jc) {
+        float sn, cs;
+        sincosf(ph[jc.value], &sn, &cs);
+        v[jc.value] = cmul(v[jc.value], make_float2(cs, conj ? -sn : sn));
+      });
+      break;
+    }
     case 7: {  // separable table: fx[x] * fy[y]
       const float* fx = reinterpret_cast<const float*>(mask);
       const float fy = __ldg(fx + N + y);
@@ -245,7 +256,7 @@ __device__ __forceinline__ void apply_mask_row(float2 (&v)[16], const void* mask
       });
       break;
     }
-    default: {  // phase, float64, complex128: rolled
+    default: {  // float64, complex128: rolled
 #pragma unroll 1
       for (int j = 0; j < 16; ++j) {
         float2 m = mask_value_xy(mask, type, y, t + T * j, N);

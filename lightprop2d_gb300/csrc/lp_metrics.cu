@@ -9,7 +9,7 @@
 // from the centre; the caller scales by dL).  The second moments are taken
 // about the centroid, as the reference does, so an off-centre beam loses no
 // precision to cancellation.  Each thread accumulates in FP32 over a strided
-// share of the grid (a few hundred points at most), then warps and CTAs
+// share of the grid (8 loads in flight, tens of points), then warps and CTAs
 // reduce in FP64 and one atomicAdd per CTA lands in the 5-double result.
 #include <cuda_runtime.h>
 
@@ -20,8 +20,11 @@
 
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kUnroll = 4;  // loads in flight per thread
+// One 1024-thread CTA per SM with 8 loads in flight per thread keeps ~10 MB
+// in flight on GB300; few CTAs keep the final FP64 atomics (3 per CTA onto
+// the same 40 bytes) from contending.
+constexpr int kThreads = 1024;
+constexpr int kUnroll = 8;  // loads in flight per thread
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -129,9 +132,9 @@ extern "C" lp_status lp_beam_moments(const lp_cfloat* field, int n, double* mome
   int logn = 0;
   while ((1 << logn) < n) ++logn;
   const size_t n2 = (size_t)n * n;
-  const size_t want = (n2 + kThreads * 16 - 1) / (kThreads * 16);  // >= 16 points a thread
-  const int grid = (int)(want < (size_t)g_sms_metrics * 4 ? (want ? want : 1)
-                                                          : (size_t)g_sms_metrics * 4);
+  const size_t want = (n2 + kThreads * kUnroll - 1) / (kThreads * kUnroll);
+  const int grid = (int)(want < (size_t)g_sms_metrics ? (want ? want : 1)
+                                                      : (size_t)g_sms_metrics);
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e = cudaMemsetAsync(moments, 0, 5 * sizeof(double), st);
   if (e == cudaSuccess) {
