@@ -115,7 +115,7 @@ BATCH_MIX = ((256, 2621), (512, 1024), (1024, 369), (2048, 82))
 BATCH_WL = 632e-7
 
 
-def batch_workload(dev, seed=3, mix=BATCH_MIX):
+def batch_workload(dev, seed=3, mix=BATCH_MIX, scale=1.0):
     """Seeded uneven-size batch, generated on the device: per beam a round
     hole of radius U[0.05, 0.40]*A (amplitude U[0,1), phase U[0,2pi)), area
     A = U[200 um, 2 mm], lens f = U[1, 20] cm, z = U[0.5, 20] cm, wl 632 nm.
@@ -128,6 +128,7 @@ def batch_workload(dev, seed=3, mix=BATCH_MIX):
     out = {k: [] for k in ("fields", "iprofiles", "area", "z", "f", "n")}
     out["stacks"] = []
     for n, cnt in mix:
+        cnt = max(1, int(round(cnt * scale)))
         frac = rng.uniform(0.05, 0.40, cnt)
         out["area"] += list(rng.uniform(200e-4, 0.2, cnt))
         out["f"] += list(rng.uniform(1.0, 20.0, cnt))
@@ -151,9 +152,12 @@ def batch_workload(dev, seed=3, mix=BATCH_MIX):
     return out
 
 
-def batch_section(dev, stream, clocks, reps, check_oracle=True):
+def batch_section(dev, stream, clocks, reps, check_oracle=True, scale=1.0, compare=True):
     """Config: the uneven batch as one persistent launch in a CUDA graph
-    (autotuned options), against the same beams as per-beam fused calls."""
+    (autotuned options), against the same beams as per-beam fused calls.
+    Parity: sampled beams against the oracle, and for every beam energy
+    conservation (the lens and H are unimodular: sum |u|^2 before equals
+    sum of the iprofile after, to FFT round-off)."""
     import torch
     from lightprop2d_gb300 import _lib as L
     from lightprop2d_gb300 import backend as B
@@ -161,8 +165,10 @@ def batch_section(dev, stream, clocks, reps, check_oracle=True):
     from lightprop2d_gb300.batch import BeamBatch
     from oracle import lp_oracle as O
 
-    W = batch_workload(dev)
+    W = batch_workload(dev, scale=scale)
     nb, pts = len(W["fields"]), sum(n * n for n in W["n"])
+    e_in = torch.cat([(st.real ** 2 + st.imag ** 2).sum((1, 2), dtype=torch.float64)
+                      for st, _ in W["stacks"]])
     # parity sample: first beam of every size, kept on the host before any run
     pick = [W["n"].index(n) for n, _ in BATCH_MIX]
     keep = {i: W["fields"][i].cpu().numpy() for i in pick}
@@ -179,11 +185,16 @@ def batch_section(dev, stream, clocks, reps, check_oracle=True):
             x, _ = O.lens(keep[i].astype(np.complex128), g["X"], g["Y"], g["k0"], W["f"][i])
             _, x = O.propagate(O.fft2(x), g["Kz"], W["z"][i])
             errs[str(n)] = O.rel_l2(W["fields"][i].cpu().numpy(), x)
+    e_out = torch.cat([ip.sum((1, 2), dtype=torch.float64) for _, ip in W["stacks"]])
+    energy_err = float(((e_out - e_in).abs() / e_in).max())
     bb.close()
     del keep
 
-    with clocks.window():
-        best, table = tune.autotune_batch(W["fields"], *args, reps=3)
+    if compare:
+        with clocks.window():
+            best, table = tune.autotune_batch(W["fields"], *args, reps=3)
+    else:
+        best, table = {}, {}
     bb = BeamBatch(W["fields"], *args, **best)
     info = bb.info()
     graph = bb.capture()
@@ -203,6 +214,12 @@ def batch_section(dev, stream, clocks, reps, check_oracle=True):
     with clocks.window():
         t_graph = ev_time(graph.replay, reps)
     bb.status()
+
+    if not compare:
+        bb.close()
+        del graph
+        return {"beams": nb, "points": pts, "ms_per_batch": round(t_graph, 4),
+                "energy_rel_err_max_all_beams": energy_err, "rel_l2_vs_fp64_oracle": errs}
 
     # the same beams as one fused field->field call each (3 launches per beam)
     fl, ipl = W["fields"], W["iprofiles"]
@@ -240,6 +257,7 @@ def batch_section(dev, stream, clocks, reps, check_oracle=True):
         "per_beam_calls_graph_ms": round(t_calls_graph, 4),
         "speedup_vs_per_beam_graph": round(t_calls_graph / t_graph, 3),
         "rel_l2_vs_fp64_oracle": errs,
+        "energy_rel_err_max_all_beams": energy_err,
         "l2": f"{pts * 8 / 2**30:.1f} GiB of fields per batch (> L2)",
     }
 
@@ -404,6 +422,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--quick", action="store_true", help="skip the sweep")
+    ap.add_argument("--only", choices=["batch", "next_rows"],
+                    help="run one section once and print its JSON (profiling cases)")
+    ap.add_argument("--batch-scale", type=float, default=1.0,
+                    help="beam counts of the uneven batch times this factor (--only batch)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
@@ -415,7 +437,7 @@ def main():
 
     # CPU baseline first (spawned pool, before any CUDA work in this process).
     cb = None
-    if rank == 0 and world == 1 and not args.no_cpu:
+    if rank == 0 and world == 1 and not args.no_cpu and not args.only:
         cb = cpu_baseline(steps=3)
 
     import torch
@@ -521,6 +543,15 @@ def main():
         return step, passes
 
     clocks = ClockSampler(local)
+    if args.only:
+        # one section, once (the cases the committed ncu summaries profile)
+        if args.only == "batch":
+            res = batch_section(dev, stream, clocks, reps=2, check_oracle=False,
+                                scale=args.batch_scale, compare=False)
+        else:
+            res = next_rows_section(dev, stream, peaks()[0])
+        print(json.dumps({"section": args.only, **res}))
+        return 0
     clocks.start()
     time.sleep(0.3)
 
