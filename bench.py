@@ -485,6 +485,8 @@ def main():
         f = torch.as_tensor(O.gaussian(n, AREA, 1.0, WAIST).astype(np.complex64), device=dev)
         return [(f.clone(), torch.empty_like(f)) for _ in range(slots)]
 
+    ranks_in_step = {"on": True}  # False inside rank-0-only sections (no barriers)
+
     def timed(fn, steps, warmup, npass=0, flush_l2=False):
         """CUDA-event timing on the launching stream.  fn(i) runs step i.
 
@@ -502,7 +504,7 @@ def main():
         torch.cuda.synchronize()
         if not npass and not flush_l2:
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            if dist:
+            if dist and ranks_in_step["on"]:
                 dist.barrier()
             torch.cuda.synchronize()
             a.record(stream)
@@ -510,7 +512,7 @@ def main():
                 L.check(fn(i), "timed step")
             b.record(stream)
             torch.cuda.synchronize()
-            if dist:
+            if dist and ranks_in_step["on"]:
                 dist.barrier()
             tot = a.elapsed_time(b)
             return [tot / steps] * steps, []
@@ -520,7 +522,7 @@ def main():
             for e in row:
                 e.record(stream)
         torch.cuda.synchronize()
-        if dist:
+        if dist and ranks_in_step["on"]:
             dist.barrier()
         torch.cuda.synchronize()
         for i in range(steps):
@@ -536,7 +538,7 @@ def main():
                 evs[i][1].record(stream)
         lib.lp_profile_events(None, 0)
         torch.cuda.synchronize()
-        if dist:
+        if dist and ranks_in_step["on"]:
             dist.barrier()
         step = [row[0].elapsed_time(row[-1]) for row in evs]
         passes = [[row[p].elapsed_time(row[p + 1]) for row in evs] for p in range(npass)]
@@ -600,6 +602,7 @@ def main():
 
     # ------------------------------------------------------------ variants --
     if rank == 0 and not args.quick:
+        ranks_in_step["on"] = False  # only rank 0 runs this section
         ks = max(10, min(200, args.steps // 10))
         specs = [B.fft2(fi) for fi, _ in slots]
         with clocks.window():

@@ -69,7 +69,7 @@ def batch_signature(fields) -> tuple:
 
 
 def autotune_batch(fields, area_size, wl, z, lens_f=0.0, iprofiles=None, reps: int = 3,
-                   ctas=(1, 2), tiles_per_item=(4, 8, 16), group_points_log2=(21, 23, 25)):
+                   ctas=(1, 2), tiles_per_item=(4, 8, 16), group_points_log2=(21, 22, 23, 24)):
     """Time the batch for every candidate option set and return
     (best options dict, {options tuple: ms}).  The fields are transformed in
     place by every timed run: pass scratch copies.  Cached per signature."""
