@@ -57,7 +57,10 @@ def design_phase_mask(n=1024, area=0.1, wl=1064e-7, waist=300e-4, z=10.0, steps=
     target = spot_target(n, area, n_spots, spot_waist, seed, device)
     power = float((field.abs() ** 2).sum())
     target = target * (power / float(target.sum()))
-    opt = torch.optim.Adam([phase], lr=lr)
+    try:
+        opt = torch.optim.Adam([phase], lr=lr, fused=True)
+    except (TypeError, RuntimeError):
+        opt = torch.optim.Adam([phase], lr=lr)
     losses = []
     for it in range(steps):
         opt.zero_grad(set_to_none=True)
@@ -66,10 +69,10 @@ def design_phase_mask(n=1024, area=0.1, wl=1064e-7, waist=300e-4, z=10.0, steps=
         loss = ((inten - target) ** 2).mean()
         loss.backward()
         opt.step()
-        losses.append(float(loss.detach()))
+        losses.append(loss.detach())          # no host sync inside the loop
         if callback is not None:
-            callback(it, losses[-1])
-    return phase.detach(), losses
+            callback(it, float(losses[-1]))
+    return phase.detach(), [float(v) for v in torch.stack(losses).cpu()]
 
 
 def gaussian_screens(k, n, area, corr_len=200e-4, rms=1.0, seed=0, device="cuda"):
