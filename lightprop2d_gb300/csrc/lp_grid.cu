@@ -91,25 +91,39 @@ __device__ __forceinline__ void axis_pos(int j, int half, float r_hi, float r_lo
   w = frac;
 }
 
-__global__ void crop_kernel(const float2* __restrict__ in, int n_in, int k0, int n_keep,
-                            float2* __restrict__ out, int n_out, float r_hi, float r_lo,
-                            float o_hi, float o_lo) {
-  const size_t total = (size_t)n_out * n_out;
+// One CTA per group of output rows: the column positions (window index and
+// weight) are computed once per CTA into shared memory, the row position
+// once per row, so a point costs four gathers and a bilinear blend.
+constexpr int kMaxOut = 4096;
+
+__global__ void __launch_bounds__(kThreads) crop_kernel(const float2* __restrict__ in, int n_in,
+                                                        int k0, int n_keep,
+                                                        float2* __restrict__ out, int n_out,
+                                                        float r_hi, float r_lo, float o_hi,
+                                                        float o_lo) {
+  __shared__ int s_ix[kMaxOut];
+  __shared__ float s_wx[kMaxOut];
   const int half = n_out / 2;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / n_out), x = (int)(i % n_out);
-    int ix, iy;
-    float wx, wy;
-    axis_pos(x, half, r_hi, r_lo, o_hi, o_lo, n_keep, ix, wx);
+  for (int x = threadIdx.x; x < n_out; x += kThreads)
+    axis_pos(x, half, r_hi, r_lo, o_hi, o_lo, n_keep, s_ix[x], s_wx[x]);
+  __syncthreads();
+  for (int y = blockIdx.x; y < n_out; y += gridDim.x) {
+    int iy;
+    float wy;
     axis_pos(y, half, r_hi, r_lo, o_hi, o_lo, n_keep, iy, wy);
-    const int ix1 = min(ix + 1, n_keep - 1), iy1 = min(iy + 1, n_keep - 1);
+    const int iy1 = min(iy + 1, n_keep - 1);
     const float2* r0 = in + (size_t)(k0 + iy) * n_in + k0;
     const float2* r1 = in + (size_t)(k0 + iy1) * n_in + k0;
-    const float2 a = r0[ix], b = r0[ix1], c = r1[ix], d = r1[ix1];
-    const float ux = 1.0f - wx, uy = 1.0f - wy;
-    out[i] = make_float2(uy * (ux * a.x + wx * b.x) + wy * (ux * c.x + wx * d.x),
-                         uy * (ux * a.y + wx * b.y) + wy * (ux * c.y + wx * d.y));
+    const float uy = 1.0f - wy;
+    float2* orow = out + (size_t)y * n_out;
+    for (int x = threadIdx.x; x < n_out; x += kThreads) {
+      const int ix = s_ix[x], ix1 = min(ix + 1, n_keep - 1);
+      const float wx = s_wx[x], ux = 1.0f - wx;
+      const float2 a = __ldg(r0 + ix), b = __ldg(r0 + ix1), c = __ldg(r1 + ix),
+                   d = __ldg(r1 + ix1);
+      orow[x] = make_float2(uy * (ux * a.x + wx * b.x) + wy * (ux * c.x + wx * d.x),
+                            uy * (ux * a.y + wx * b.y) + wy * (ux * c.y + wx * d.y));
+    }
   }
 }
 
@@ -161,9 +175,10 @@ lp_status lp_crop(const lp_cfloat* in, int n_in, int first, int n_keep, double x
     return fail(LP_ERR_INVALID_ARGUMENT, "lp_crop: dL_in > 0 and finite, non-zero dL_out");
   if ((const void*)in == (const void*)out)
     return fail(LP_ERR_INVALID_ARGUMENT, "lp_crop: in and out must be different grids");
+  if (n_out > kMaxOut) return fail(LP_ERR_UNSUPPORTED_SIZE, "lp_crop: n_out <= 4096");
   const FF r = ff_from_double(dL_out / dL_in);
   const FF o = ff_from_double(x0 / dL_in);
-  crop_kernel<<<grid_for((size_t)n_out * n_out), kThreads, 0, (cudaStream_t)stream>>>(
+  crop_kernel<<<n_out < 2048 ? n_out : 2048, kThreads, 0, (cudaStream_t)stream>>>(
       reinterpret_cast<const float2*>(in), n_in, first, n_keep, reinterpret_cast<float2*>(out),
       n_out, r.hi, r.lo, o.hi, o.lo);
   return launch_check("lp_crop");
