@@ -439,6 +439,8 @@ def main():
     cb = None
     if rank == 0 and world == 1 and not args.no_cpu and not args.only:
         cb = cpu_baseline(steps=3)
+        one = cpu_baseline(steps=2, procs=1)
+        cb["one_process"] = {"value": one["value"], "cores": 1, "sample": one["sample"]}
 
     import torch
     torch.cuda.set_device(local)
