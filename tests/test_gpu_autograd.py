@@ -169,3 +169,14 @@ def test_inverse_design_reduces_loss():
                                         steps=40, lr=0.1, seed=0, spot_waist=40e-4)
     assert phase.shape == (256, 256)
     assert losses[-1] < 0.7 * losses[0]
+
+
+def test_inverse_design_graph_matches_eager():
+    """The CUDA-graph training step replays the same computation as eager."""
+    from lightprop2d_gb300 import design as D
+    kw = dict(n=256, area=0.1, wl=1064e-7, waist=300e-4, z=10.0, steps=12, lr=0.1, seed=1,
+              spot_waist=40e-4)
+    pe, le = D.design_phase_mask(**kw)
+    pg, lg = D.design_phase_mask(**kw, graph=True)
+    assert np.allclose(le, lg, rtol=1e-4), (le, lg)
+    assert torch.allclose(pe, pg, rtol=1e-4, atol=1e-4)
