@@ -214,6 +214,14 @@ def batch_section(dev, stream, clocks, reps, check_oracle=True, scale=1.0, compa
     with clocks.window():
         t_graph = ev_time(graph.replay, reps)
     bb.status()
+    # the same batch with per-beam intensity moments summed in the last pass
+    bm = BeamBatch(W["fields"], *args, **best, moments=True)
+    gm = bm.capture()
+    with clocks.window():
+        t_moments = ev_time(gm.replay, max(3, reps // 2))
+    bm.status()
+    bm.close()
+    del gm
 
     if not compare:
         bb.close()
@@ -251,6 +259,7 @@ def batch_section(dev, stream, clocks, reps, check_oracle=True, scale=1.0, compa
         "effective_gbs": round(alg / (t_graph * 1e-3) / 1e9, 1),
         "alg_bytes_per_batch": alg,
         "launches_per_batch": 1,
+        "ms_per_batch_with_moments": round(t_moments, 4),
         "plan": {**best, **info},
         "autotune_ms": {str(k): round(v, 4) for k, v in table.items()},
         "per_beam_calls_ms": round(t_calls, 4),

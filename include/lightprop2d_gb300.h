@@ -248,6 +248,13 @@ typedef struct lp_beam_desc {
   double area_size, wl, z;
   double lens_f;     /* 0: no lens */
   uint32_t flags;    /* LP_FLAG_PHASE_FP32 | LP_FLAG_EVANESCENT_MASK */
+  /* optional device array of 5 doubles, or NULL: every run sets it to the
+   * intensity moments of the result (Beam2D.centroid / D4sigma,
+   * beam2d.py:669-704) summed in the last pass's epilogue:
+   * sum I, sum jx I, sum jy I, sum jx^2 I, sum jy^2 I, with jx = ix - n/2,
+   * jy = iy - n/2 (raw moments about the grid centre; the second moments
+   * about the centroid follow by subtraction) */
+  double* moments;
 } lp_beam_desc;
 
 typedef struct lp_batch_options {

@@ -49,7 +49,8 @@ class BeamDesc(ctypes.Structure):
     """lp_beam_desc"""
     _fields_ = [("field", ctypes.c_void_p), ("iprofile", ctypes.c_void_p), ("n", ctypes.c_int),
                 ("area_size", ctypes.c_double), ("wl", ctypes.c_double), ("z", ctypes.c_double),
-                ("lens_f", ctypes.c_double), ("flags", ctypes.c_uint32)]
+                ("lens_f", ctypes.c_double), ("flags", ctypes.c_uint32),
+                ("moments", ctypes.c_void_p)]
 
 
 class BatchOptions(ctypes.Structure):

@@ -14,6 +14,7 @@ from __future__ import annotations
 import ctypes
 from typing import Sequence
 
+import numpy as np
 import torch
 
 from . import _lib as L
@@ -29,7 +30,8 @@ class BeamBatch:
     def __init__(self, fields: Sequence[torch.Tensor], area_size, wl, z, lens_f=0.0,
                  iprofiles: Sequence[torch.Tensor] | None = None, flags: int = 0,
                  ctas_per_sm: int = 0, tiles_per_item: int = 0, group_points_log2: int = 0,
-                 spin_limit: int = 0, debug_unsatisfiable: bool = False):
+                 spin_limit: int = 0, debug_unsatisfiable: bool = False,
+                 moments: bool = False):
         nb = len(fields)
         if nb == 0:
             raise ValueError("empty batch")
@@ -45,6 +47,10 @@ class BeamBatch:
             per(lens_f, "lens_f")
         descs = (L.BeamDesc * nb)()
         self.fields = list(fields)
+        self.areas = areas
+        # per-beam intensity moments summed in the last pass (see metrics())
+        self.moments = (torch.zeros((nb, 5), dtype=torch.float64, device=self.fields[0].device)
+                        if moments else None)
         self.iprofiles = list(iprofiles) if iprofiles is not None else [None] * nb
         dev = self.fields[0].device
         for i, f in enumerate(self.fields):
@@ -55,8 +61,9 @@ class BeamBatch:
             if ip is not None and not (ip.is_cuda and ip.dtype == torch.float32
                                        and tuple(ip.shape) == tuple(f.shape)):
                 raise ValueError(f"iprofile {i}: float32 CUDA tensor of the field's shape")
+            mp = self.moments[i].data_ptr() if self.moments is not None else 0
             descs[i] = L.BeamDesc(f.data_ptr(), ip.data_ptr() if ip is not None else 0,
-                                  f.shape[0], areas[i], wls[i], zs[i], fs[i], int(flags))
+                                  f.shape[0], areas[i], wls[i], zs[i], fs[i], int(flags), mp)
         opts = L.BatchOptions(int(ctas_per_sm), int(tiles_per_item), int(group_points_log2),
                               int(spin_limit), int(bool(debug_unsatisfiable)))
         self.device = dev
@@ -87,6 +94,24 @@ class BeamBatch:
         L.check(self._lib.lp_batch_info(self._h, ctypes.byref(n), ctypes.byref(g),
                                         ctypes.byref(c)), "lp_batch_info")
         return {"items": n.value, "grid": g.value, "ctas_per_sm": c.value}
+
+    def metrics(self):
+        """Per-beam (Xc, Yc, D4sigma_x, D4sigma_y) in cm after a run, from the
+        moments summed in the last pass (Beam2D.centroid / D4sigma,
+        beam2d.py:669-704).  The widths use raw moments about the grid
+        centre: the relative error grows like (offset / width)^2 * 1e-7, so
+        beams far off centre relative to their width should use
+        Beam2D.D4sigma (second moments about the centroid)."""
+        if self.moments is None:
+            raise ValueError("BeamBatch(..., moments=True) is needed for metrics()")
+        m = self.moments.cpu().numpy()
+        n = np.array([f.shape[0] for f in self.fields], dtype=np.float64)
+        dL = np.asarray(self.areas, dtype=np.float64) / n
+        with np.errstate(invalid="ignore", divide="ignore"):
+            xc, yc = m[:, 1] / m[:, 0], m[:, 2] / m[:, 0]
+            vx = np.maximum(m[:, 3] / m[:, 0] - xc ** 2, 0.0)
+            vy = np.maximum(m[:, 4] / m[:, 0] - yc ** 2, 0.0)
+        return np.stack([dL * xc, dL * yc, 4 * dL * np.sqrt(vx), 4 * dL * np.sqrt(vy)], axis=1)
 
     def capture(self) -> torch.cuda.CUDAGraph:
         """Capture one run into a CUDA graph (replay with graph.replay())."""

@@ -155,6 +155,10 @@ __global__ void __launch_bounds__(kBT) batch_kernel(const BeamRec* __restrict__ 
     const Item item = items[s_item];
     const BeamRec* bp = beams + item.beam;
     const int n = bp->n;
+    // The column pass's first item clears the beam's moment sums; every
+    // row-pass-2 item runs after all column items (dependency counter).
+    if (item.pass == 1 && item.tile0 == 0 && threadIdx.x < 5 && bp->inv.moments)
+      bp->inv.moments[threadIdx.x] = 0.0;
     if (n != cur_n) {  // stage twiddles of this size into shared memory
       const float2* src = tw_tables[31 - __clz(n)];
       const int cnt = tw_count(n);
@@ -253,6 +257,8 @@ lp_status lp_batch_create(const lp_beam_desc* beams, int count, const lp_batch_o
       return fail(LP_ERR_MISALIGNED, "beam field must be 8-byte aligned");
     if (b.iprofile && (reinterpret_cast<uintptr_t>(b.iprofile) & 3u))
       return fail(LP_ERR_MISALIGNED, "beam iprofile must be 4-byte aligned");
+    if (b.moments && (reinterpret_cast<uintptr_t>(b.moments) & 7u))
+      return fail(LP_ERR_MISALIGNED, "beam moments must be 8-byte aligned");
     if (!(b.area_size > 0 && b.wl > 0) || !std::isfinite(b.z) || !std::isfinite(b.lens_f))
       return fail(LP_ERR_INVALID_ARGUMENT, "beam geometry must be finite, area and wl > 0");
     if (b.flags & ~(uint32_t)(LP_FLAG_PHASE_FP32 | LP_FLAG_EVANESCENT_MASK))
@@ -285,6 +291,7 @@ lp_status lp_batch_create(const lp_beam_desc* beams, int count, const lp_batch_o
     r.col.scale = 1.0f / ((float)b.n * (float)b.n);
     r.inv = row_ops_none();
     r.inv.iprofile = b.iprofile;
+    r.inv.moments = b.moments;
   }
 
   // Work queue: groups of ~2^glog points; pass p of group g is queued after

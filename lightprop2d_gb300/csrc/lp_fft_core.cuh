@@ -336,6 +336,43 @@ __device__ __forceinline__ void load_row(float2 (&v)[16], const float2* in, int 
   static_for<16>([&](auto jc) { v[decltype(jc)::value] = gld<CG>(src + T * decltype(jc)::value); });
 }
 
+// Intensity moments of the thread's 16 points of row y (columns t + T*j),
+// reduced over the exchange group (FP32 per thread, FP64 across lanes and
+// warps) and added to out[0..5) with one atomic per value per group:
+// sum I, sum jx I, sum jy I, sum jx^2 I, sum jy^2 I (offsets from the centre).
+template <int N, int SY>
+__device__ __forceinline__ void tile_moments(const float2 (&v)[16], int y, int t, double* out) {
+  constexpr int T = FftGeo<N>::T;
+  float s0 = 0.0f, s1 = 0.0f, s3 = 0.0f;
+  static_for<16>([&](auto jc) {
+    constexpr int j = decltype(jc)::value;
+    const float I = fmaf(v[j].x, v[j].x, v[j].y * v[j].y);
+    const float jx = (float)(t + T * j - N / 2);
+    s0 += I;
+    s1 = fmaf(jx, I, s1);
+    s3 = fmaf(jx * jx, I, s3);
+  });
+  const double jy = (double)(y - N / 2);
+  double m[5] = {(double)s0, (double)s1, jy * s0, (double)s3, jy * jy * s0};
+  __shared__ double red[2][5][8];  // [group][value][warp of the group]
+  const int tid = group_tid<SY>(), lane = tid & 31, w = tid >> 5;
+  const int grp = SY == 2 ? (int)(threadIdx.x >> 8) : 0;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m[k] += __shfl_down_sync(0xffffffffu, m[k], o);
+    if (lane == 0) red[grp][k][w] = m[k];
+  }
+  group_sync<SY>();
+  if (tid < 5) {
+    double a = 0.0;
+    const int nw = (SY == 2 ? 256 : (int)blockDim.x) >> 5;
+    for (int i = 0; i < nw && i < 8; ++i) a += red[grp][tid][i];
+    atomicAdd(out + tid, a);
+  }
+  group_sync<SY>();
+}
+
 // Row tile: rows tile*L .. tile*L+L-1 by the first L*T threads of the
 // exchange group (SY: the CTA, or a 256-thread group), thread (line
 // g = tid / T, t = tid % T).  v holds the thread's loaded points of row
@@ -373,6 +410,9 @@ __device__ __forceinline__ void row_tile(float2 (&v)[16], float2* out, int tile,
       constexpr int j = decltype(jc)::value;
       ip[T * j] = fmaf(v[j].x, v[j].x, v[j].y * v[j].y);
     });
+  }
+  if constexpr (NT >= 32) {  // whole warps (the batch kernel uses 256 threads)
+    if (ops.moments) tile_moments<N, SY>(v, y, t, ops.moments);
   }
 }
 

@@ -23,6 +23,9 @@ struct RowOps {
   // Epilogue.
   float scale;               // real factor on the output (1 = none)
   float* iprofile;           // optional |out|^2 (float32)
+  // optional: += sum I, sum jx I, sum jy I, sum jx^2 I, sum jy^2 I over the
+  // tile (I = |out|^2, jx / jy = offsets from the grid centre), FP64
+  double* moments;
 };
 
 // Work folded into a column (y-direction) pass at the spectral point.

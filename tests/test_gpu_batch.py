@@ -185,3 +185,24 @@ def test_invalid_inputs(lpb):
         lpb.BeamBatch([f], 1.0, 1e-4, 1.0, flags=0x4)
     with pytest.raises(ValueError):
         lpb.BeamBatch([f.to(torch.complex128)], 1.0, 1e-4, 1.0)
+
+
+def test_moments_in_last_pass(lpb):
+    """Per-beam centroid and D4sigma summed in the batch's last pass match the
+    oracle's restatement of Beam2D.centroid / D4sigma on each result, and are
+    re-zeroed by every run (graph replays)."""
+    beams = make_beams([512, 256, 1024, 128, 2048], seed=21)
+    fields, ips = to_dev(beams)
+    bb = make_batch(lpb, beams, fields, ips, moments=True)
+    g = bb.capture()
+    for _ in range(2):
+        g.replay()
+        bb.status()
+        met = bb.metrics()
+        for k, (b, f) in enumerate(zip(beams, fields)):
+            x = f.cpu().numpy().astype(np.complex128)
+            dL = b["area"] / b["n"]
+            Xc, Yc, _, _ = O.centroid(x, dL)
+            dx, dy = O.d4sigma(x, dL)
+            assert abs(met[k, 0] - Xc) < 1e-4 * dL and abs(met[k, 1] - Yc) < 1e-4 * dL, k
+            assert np.allclose(met[k, 2:], [dx, dy], rtol=1e-4), (k, met[k], dx, dy)
