@@ -43,6 +43,11 @@ N_HEAD, AREA, WL, WAIST, Z = 2048, 0.2, 632e-7, 100e-4, 1.0
 # workload with caches kept warm between launches (a live step's L2 state):
 # the column pass reads its input from L2 and only writes back evictions.
 NCU_DRAM_BYTES_2048 = {"row_fwd": 58.66e6, "col_fwd_H_inv": 13.12e6, "row_inv": 0.64e6}
+# The same kernels' FP32 (FMA) pipe and issue activity from an ncu --set full
+# capture of this workload: the FFT passes are bound on-chip, not by DRAM.
+NCU_PIPES_2048 = {"col_fwd_H_inv": {"fma_pipe_active_pct": 32.1, "issue_active_pct": 37.8},
+                  "row_fwd": {"fma_pipe_active_pct": 20.9, "issue_active_pct": 22.8},
+                  "row_inv": {"fma_pipe_active_pct": 21.0, "issue_active_pct": 23.5}}
 METRIC = "2048^2 complex64 fused field->field propagates/s"
 UNIT = "propagates/s"
 WORKLOAD = "gaussian beam 2048^2, area 2 mm, wl 632 nm, waist 100 um, complex64, z=1 cm/step"
@@ -796,6 +801,7 @@ def main():
                          "traffic": NCU_DRAM_BYTES_2048.get(names[dom]) if n == 2048 else None,
                          "traffic_note": "ncu dram__bytes_read+write per launch, warm L2",
                          "step_dram_bytes_ncu": sum(NCU_DRAM_BYTES_2048.values()),
+                         "ncu_pipes": NCU_PIPES_2048.get(names[dom]) if n == 2048 else None,
                          "alg_bytes_per_launch": alg_bytes},
             "cpu_baseline": cb,
             "e2e": {"value": world * 1e3 / e2e_t, "unit": UNIT,

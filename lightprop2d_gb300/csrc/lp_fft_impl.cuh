@@ -15,9 +15,10 @@
 #ifndef LP_N
 #error "define LP_N before including lp_fft_impl.cuh"
 #endif
-// Columns per CTA of the column kernels for 1024 <= N <= 2048.
+// Columns per CTA of the column kernels for 1024 <= N <= 2048 (2048: eight
+// columns, 1024 threads, measured 41.0 vs 42.2 us against four).
 #ifndef LP_COL_C
-#define LP_COL_C 4
+#define LP_COL_C (LP_N >= 2048 ? 8 : 4)
 #endif
 // Per-size choices below were measured on GB300 (fused propagate, inputs
 // larger than L2); each can be overridden with -D for tuning experiments.
@@ -35,7 +36,7 @@
 #define LP_ROW_MINB 1
 #endif
 #ifndef LP_COL_MINB
-#define LP_COL_MINB (LP_N >= 4096 ? 1 : 2)
+#define LP_COL_MINB (LP_N >= 2048 ? 1 : 2)
 #endif
 // TMA-staged row kernels (1) or register-prefetch kernels (0); used for
 // N >= 1024 only.  TMA wins at 4096 (rows of 32 KB); at 1024-2048 the
