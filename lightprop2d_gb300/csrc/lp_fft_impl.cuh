@@ -15,10 +15,18 @@
 #ifndef LP_N
 #error "define LP_N before including lp_fft_impl.cuh"
 #endif
-// Columns per CTA of the column kernels for 1024 <= N <= 2048 (2048: eight
-// columns, 1024 threads, measured 41.0 vs 42.2 us against four).
-#ifndef LP_COL_C
-#define LP_COL_C (LP_N >= 2048 ? 8 : 4)
+// Columns per CTA of the column kernels for N = 1024, 2048 and 4096 (2048:
+// eight columns, 1024 threads, measured 41.0 vs 42.2 us against four; 4096:
+// four columns, 1024 threads without prefetch, 155.8 vs 192.9 us against two
+// columns with prefetch).
+#ifndef LP_COL_C1024
+#define LP_COL_C1024 4
+#endif
+#ifndef LP_COL_C2048
+#define LP_COL_C2048 8
+#endif
+#ifndef LP_COL_C4096
+#define LP_COL_C4096 4
 #endif
 // Per-size choices below were measured on GB300 (fused propagate, inputs
 // larger than L2); each can be overridden with -D for tuning experiments.
@@ -28,7 +36,7 @@
 #define LP_ROW_PREFETCH 1
 #endif
 #ifndef LP_COL_PREFETCH
-#define LP_COL_PREFETCH (LP_N >= 4096)
+#define LP_COL_PREFETCH 0
 #endif
 // Minimum resident CTAs per SM requested from the register allocator
 // (2 with 512-thread column CTAs caps them at 64 registers).
@@ -59,7 +67,10 @@ struct Geo : FftGeo<N> {
   // rows per CTA: 256 threads for large N, one warp's worth for small N
   static constexpr int ROWS = N >= 1024 ? cmax(1, 256 / F::T) : cmin(N, cmax(1, 32 / F::T));
   // columns per CTA: at least 4 so every row segment is a full 32-byte sector
-  static constexpr int COLS = N >= 4096 ? 2 : N >= 1024 ? LP_COL_C : cmin(N, cmax(4, 32 / F::T));
+  static constexpr int COLS = N >= 4096   ? LP_COL_C4096
+                              : N >= 2048 ? LP_COL_C2048
+                              : N >= 1024 ? LP_COL_C1024
+                                          : cmin(N, cmax(4, 32 / F::T));
   static constexpr int ROW_THREADS = ROWS * F::T;
   static constexpr int COL_THREADS = COLS * F::T;
   static constexpr int ROW_UNITS = N / ROWS;
