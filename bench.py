@@ -42,12 +42,12 @@ N_HEAD, AREA, WL, WAIST, Z = 2048, 0.2, 632e-7, 100e-4, 1.0
 # DRAM bytes per launch of the 2048^2 pass kernels, measured with ncu on this
 # workload with caches kept warm between launches (a live step's L2 state):
 # the column pass reads its input from L2 and only writes back evictions.
-NCU_DRAM_BYTES_2048 = {"row_fwd": 58.66e6, "col_fwd_H_inv": 13.12e6, "row_inv": 0.64e6}
+NCU_DRAM_BYTES_2048 = {"row_fwd": 58.84e6, "col_fwd_H_inv": 10.88e6, "row_inv": 0.91e6}
 # The same kernels' FP32 (FMA) pipe and issue activity from an ncu --set full
 # capture of this workload: the FFT passes are bound on-chip, not by DRAM.
-NCU_PIPES_2048 = {"col_fwd_H_inv": {"fma_pipe_active_pct": 32.1, "issue_active_pct": 37.8},
-                  "row_fwd": {"fma_pipe_active_pct": 20.9, "issue_active_pct": 22.8},
-                  "row_inv": {"fma_pipe_active_pct": 21.0, "issue_active_pct": 23.5}}
+NCU_PIPES_2048 = {"col_fwd_H_inv": {"fma_pipe_active_pct": 33.9, "issue_active_pct": 49.8},
+                  "row_fwd": {"fma_pipe_active_pct": 21.2, "issue_active_pct": 27.8},
+                  "row_inv": {"fma_pipe_active_pct": 21.1, "issue_active_pct": 28.6}}
 METRIC = "2048^2 complex64 fused field->field propagates/s"
 UNIT = "propagates/s"
 WORKLOAD = "gaussian beam 2048^2, area 2 mm, wl 632 nm, waist 100 um, complex64, z=1 cm/step"
@@ -436,8 +436,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--quick", action="store_true", help="skip the sweep")
-    ap.add_argument("--only", choices=["batch", "next_rows"],
+    ap.add_argument("--only", choices=["batch", "next_rows", "propagate"],
                     help="run one section once and print its JSON (profiling cases)")
+    ap.add_argument("--n", type=int, default=2048,
+                    help="grid size of --only propagate (fused propagates back to back)")
     ap.add_argument("--batch-scale", type=float, default=1.0,
                     help="beam counts of the uneven batch times this factor (--only batch)")
     args = ap.parse_args()
@@ -566,6 +568,17 @@ def main():
         if args.only == "batch":
             res = batch_section(dev, stream, clocks, reps=2, check_oracle=False,
                                 scale=args.batch_scale, compare=False)
+        elif args.only == "propagate":
+            nn = args.n
+            rr = nslots(nn)
+            sl = make(nn, rr)
+            sm, _ = timed(lambda i: fused(nn, *sl[i % rr]), args.steps, args.warmup)
+            _, pm = timed(lambda i: fused(nn, *sl[i % rr]), args.steps, 3, 3)
+            ms = statistics.fmean(sm)
+            res = {"n": nn, "ms": round(ms, 5), "propagates_per_s": round(1e3 / ms, 1),
+                   "effective_gbs": round(16 * nn * nn / (ms * 1e-3) / 1e9, 1),
+                   "passes_ms": [round(statistics.fmean(p), 5) for p in pm],
+                   "slots": rr}
         else:
             res = next_rows_section(dev, stream, peaks()[0])
         print(json.dumps({"section": args.only, **res}))
