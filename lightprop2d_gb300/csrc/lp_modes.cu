@@ -8,10 +8,10 @@
 //
 // Both are matrix-vector products over an M x P complex64 basis (P = nb^2):
 // HBM-bound (every basis element is read once, 8 B, for 8 flops), so they are
-// CUDA-core kernels reading the basis with coalesced loads, several in flight
-// per thread, not tensor-core GEMMs.  Sums run in FP32 over short runs (4
-// terms in the projection, 16 in the synthesis) and in FP64 across runs, so
-// results carry FP32 rounding of the inputs only.
+// CUDA-core kernels streaming the basis with coalesced loads, many in flight
+// per thread, not tensor-core GEMMs.  Products are summed in FP32 over runs of
+// 16 terms and the runs in FP64, so results carry FP32 rounding of the
+// inputs only (GB300's FP64 rate is far too low for one FP64 add per term).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -24,7 +24,20 @@ using namespace lp;
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kChunk = 1 << 16;  // basis points per CTA of the projection
+// Projection tiling: kModes modes per CTA, kPts window points per thread per
+// step (kModes * kPts basis loads in flight), kChunk window points per CTA,
+// FP32 runs of kRun steps.  Measured on GB300 (256 modes x 1024^2): 4 x 4 at
+// 80 registers 356 us, 8 x 2 427 us, 8 x 4 493 us, 2 x 8 369 us.
+#ifndef LP_MODES_MB
+#define LP_MODES_MB 4
+#endif
+#ifndef LP_MODES_PT
+#define LP_MODES_PT 4
+#endif
+constexpr int kModes = LP_MODES_MB;
+constexpr int kPts = LP_MODES_PT;
+constexpr int kChunk = 1 << 14;
+constexpr int kRun = 16 / kPts;
 
 lp_status fail(lp_status s, const char* msg) { return (lp_status)set_last_error((int)s, msg); }
 
@@ -34,69 +47,89 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// grid (chunks, modes): CTA (ck, m) adds sum over points [ck*kChunk, ...) of
-// modes[m][p] * w[p] into c[m] (FP64 pair).
+// grid (chunks, ceil(M / kModes)): CTA (ck, g) adds, for modes
+// m = g*kModes .. +kModes-1, the sum over window points [ck*kChunk, ...) of
+// modes[m][p] * w[p] into c[m] (FP64 pair).  Each thread reads a field value
+// once for all kModes modes; window point p = r*nb + q is field element
+// (first + r, first + q), with (r, q) advanced incrementally (P < 2^31).
 __global__ void __launch_bounds__(kThreads) project_kernel(const float2* __restrict__ modes,
-                                                           long long P, int nb,
+                                                           int M, int P, int nb,
                                                            const float2* __restrict__ field,
                                                            int n, int first,
                                                            double* __restrict__ c) {
-  const int m = blockIdx.y;
-  const long long p0 = (long long)blockIdx.x * kChunk;
-  const long long p1 = p0 + kChunk < P ? p0 + kChunk : P;
-  const float2* row = modes + (size_t)m * P;
-  double ar = 0.0, ai = 0.0;
-  // (r, q) of point p tracked incrementally (no division in the loop)
-  long long p = p0 + threadIdx.x;
-  int r = (int)(p / nb), q = (int)(p - (long long)r * nb);
-  while (p < p1) {
-    float fr = 0.0f, fi = 0.0f;
-    float2 a[4], w[4];
-    bool ok[4];
+  const int m0 = blockIdx.y * kModes;
+  const int mc = M - m0 < kModes ? M - m0 : kModes;
+  const int p0 = blockIdx.x * kChunk;
+  const int p1 = P - p0 > kChunk ? p0 + kChunk : P;
+  const float2* base = modes + (size_t)m0 * P;
+  const float2* frow = field + (size_t)first * n + first;
+  double tr[kModes], ti[kModes];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {  // four independent pairs of loads in flight
-      ok[u] = p < p1;
-      a[u] = ok[u] ? __ldg(row + p) : make_float2(0.0f, 0.0f);
-      w[u] = ok[u] ? __ldg(field + (size_t)(first + r) * n + first + q) : make_float2(0.0f, 0.0f);
-      p += kThreads;
-      q += kThreads;
-      while (q >= nb) {
-        q -= nb;
-        ++r;
+  for (int k = 0; k < kModes; ++k) tr[k] = ti[k] = 0.0;
+  int p = p0 + threadIdx.x;
+  int r = p / nb, q = p - r * nb;
+  while (p < p1) {
+    float fr[kModes], fi[kModes];
+#pragma unroll
+    for (int k = 0; k < kModes; ++k) fr[k] = fi[k] = 0.0f;
+#pragma unroll 1
+    for (int it = 0; it < kRun && p < p1; ++it) {
+      float2 w[kPts], a[kPts][kModes];
+#pragma unroll
+      for (int u = 0; u < kPts; ++u) {
+        const int pu = p + u * kThreads;
+        const bool ok = pu < p1;
+        w[u] = ok ? __ldg(frow + (size_t)r * n + q) : make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int k = 0; k < kModes; ++k)
+          a[u][k] = ok && k < mc ? __ldg(base + (size_t)k * P + pu) : make_float2(0.0f, 0.0f);
+        q += kThreads;
+        while (q >= nb) {
+          q -= nb;
+          ++r;
+        }
+      }
+      p += kPts * kThreads;
+#pragma unroll
+      for (int u = 0; u < kPts; ++u) {
+#pragma unroll
+        for (int k = 0; k < kModes; ++k) {
+          fr[k] = fmaf(a[u][k].x, w[u].x, fmaf(-a[u][k].y, w[u].y, fr[k]));
+          fi[k] = fmaf(a[u][k].x, w[u].y, fmaf(a[u][k].y, w[u].x, fi[k]));
+        }
       }
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      fr = fmaf(a[u].x, w[u].x, fmaf(-a[u].y, w[u].y, fr));
-      fi = fmaf(a[u].x, w[u].y, fmaf(a[u].y, w[u].x, fi));
+    for (int k = 0; k < kModes; ++k) {
+      tr[k] += fr[k];
+      ti[k] += fi[k];
     }
-    ar += fr;
-    ai += fi;
   }
-  __shared__ double part[2][kThreads / 32];
+  __shared__ double part[2 * kModes][kThreads / 32];
   const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
-  ar = warp_sum(ar);
-  ai = warp_sum(ai);
-  if (lane == 0) {
-    part[0][wi] = ar;
-    part[1][wi] = ai;
+#pragma unroll
+  for (int k = 0; k < kModes; ++k) {
+    const double sr = warp_sum(tr[k]), si = warp_sum(ti[k]);
+    if (lane == 0) {
+      part[2 * k][wi] = sr;
+      part[2 * k + 1][wi] = si;
+    }
   }
   __syncthreads();
-  if (threadIdx.x < 32) {
-    double sr = threadIdx.x < kThreads / 32 ? part[0][threadIdx.x] : 0.0;
-    double si = threadIdx.x < kThreads / 32 ? part[1][threadIdx.x] : 0.0;
-    sr = warp_sum(sr);
-    si = warp_sum(si);
-    if (threadIdx.x == 0) {
-      atomicAdd(c + 2 * m, sr);
-      atomicAdd(c + 2 * m + 1, si);
-    }
+  if (threadIdx.x < 2 * mc) {
+    double acc = 0.0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) acc += part[threadIdx.x][w];
+    atomicAdd(c + 2 * m0 + threadIdx.x, acc);
   }
 }
 
-// One thread per field point: inside the window sum_m c[m]*modes[m][p], else 0.
-// The coefficients are staged through shared memory in blocks of kCoef.
+// One thread per window point: sum_m c[m] * modes[m][p], with 16 basis loads
+// issued before they are used; the coefficients are staged through shared
+// memory in blocks of kCoef.  Points outside the window were zeroed by the
+// caller.
 constexpr int kCoef = 512;
+constexpr int kBlk = 16;
 
 __global__ void __launch_bounds__(kThreads) combine_kernel(const float2* __restrict__ modes,
                                                            int M, long long P, int nb,
@@ -104,14 +137,10 @@ __global__ void __launch_bounds__(kThreads) combine_kernel(const float2* __restr
                                                            float2* __restrict__ field, int n,
                                                            int first) {
   __shared__ float2 cs[kCoef];
-  const size_t total = (size_t)n * n;
-  for (size_t base = (size_t)blockIdx.x * kThreads; base < total;
-       base += (size_t)gridDim.x * kThreads) {
-    const size_t i = base + threadIdx.x;
-    const int y = (int)(i / n), x = (int)(i % n);
-    const int r = y - first, q = x - first;
-    const bool in = i < total && r >= 0 && r < nb && q >= 0 && q < nb;
-    const long long p = (long long)r * nb + q;
+  for (long long base = (long long)blockIdx.x * kThreads; base < P;
+       base += (long long)gridDim.x * kThreads) {
+    const long long p = base + threadIdx.x;
+    const bool in = p < P;
     double sr = 0.0, si = 0.0;
     for (int m0 = 0; m0 < M; m0 += kCoef) {
       const int mc = M - m0 < kCoef ? M - m0 : kCoef;
@@ -120,23 +149,34 @@ __global__ void __launch_bounds__(kThreads) combine_kernel(const float2* __restr
         cs[j] = make_float2((float)c[2 * (m0 + j)], (float)c[2 * (m0 + j) + 1]);
       __syncthreads();
       if (in) {
-        float fr = 0.0f, fi = 0.0f;
-        for (int j = 0; j < mc; ++j) {
-          const float2 a = __ldg(modes + (size_t)(m0 + j) * P + p);
-          const float2 w = cs[j];
-          fr = fmaf(a.x, w.x, fmaf(-a.y, w.y, fr));
-          fi = fmaf(a.x, w.y, fmaf(a.y, w.x, fi));
-          if ((j & 15) == 15) {
-            sr += fr;
-            si += fi;
-            fr = fi = 0.0f;
+        const float2* col = modes + (size_t)m0 * P + p;
+#pragma unroll 1
+        for (int j0 = 0; j0 < mc; j0 += kBlk) {
+          float2 a[kBlk];
+          if (j0 + kBlk <= mc) {
+#pragma unroll
+            for (int u = 0; u < kBlk; ++u) a[u] = __ldg(col + (size_t)(j0 + u) * P);
+          } else {
+#pragma unroll
+            for (int u = 0; u < kBlk; ++u)
+              a[u] = j0 + u < mc ? __ldg(col + (size_t)(j0 + u) * P) : make_float2(0.0f, 0.0f);
           }
+          float fr = 0.0f, fi = 0.0f;
+#pragma unroll
+          for (int u = 0; u < kBlk; ++u) {
+            const float2 w = cs[j0 + u < mc ? j0 + u : 0];
+            fr = fmaf(a[u].x, w.x, fmaf(-a[u].y, w.y, fr));
+            fi = fmaf(a[u].x, w.y, fmaf(a[u].y, w.x, fi));
+          }
+          sr += fr;
+          si += fi;
         }
-        sr += fr;
-        si += fi;
       }
     }
-    if (i < total) field[i] = make_float2((float)sr, (float)si);
+    if (in) {
+      const int r = (int)(p / nb), q = (int)(p - (long long)r * nb);
+      field[(size_t)(first + r) * n + first + q] = make_float2((float)sr, (float)si);
+    }
   }
 }
 
@@ -151,6 +191,7 @@ lp_status check_common(const void* modes, int n_modes, int nb, const void* field
   if (!aligned(modes, 8) || !aligned(field, 8) || !aligned(c, 8))
     return fail(LP_ERR_MISALIGNED, "mode basis: 8-byte alignment");
   if (n_modes > 65535) return fail(LP_ERR_INVALID_ARGUMENT, "mode basis: at most 65535 modes");
+  if (nb > 46340) return fail(LP_ERR_INVALID_ARGUMENT, "mode basis: window side at most 46340");
   return LP_OK;
 }
 
@@ -166,10 +207,10 @@ lp_status lp_modes_project(const lp_cfloat* modes, int n_modes, int nb, const lp
   const long long P = (long long)nb * nb;
   cudaError_t e = cudaMemsetAsync(coeffs, 0, sizeof(double) * 2 * (size_t)n_modes, st);
   if (e != cudaSuccess) return fail(LP_ERR_CUDA, cudaGetErrorString(e));
-  const dim3 grid((unsigned)((P + kChunk - 1) / kChunk), (unsigned)n_modes);
-  project_kernel<<<grid, kThreads, 0, st>>>(reinterpret_cast<const float2*>(modes), P, nb,
-                                            reinterpret_cast<const float2*>(field), n,
-                                            (n - nb) / 2, coeffs);
+  const dim3 grid((unsigned)((P + kChunk - 1) / kChunk), (unsigned)((n_modes + kModes - 1) / kModes));
+  project_kernel<<<grid, kThreads, 0, st>>>(reinterpret_cast<const float2*>(modes), n_modes,
+                                            (int)P, nb, reinterpret_cast<const float2*>(field),
+                                            n, (n - nb) / 2, coeffs);
   e = cudaGetLastError();
   return e == cudaSuccess ? LP_OK : fail(LP_ERR_CUDA, cudaGetErrorString(e));
 }
@@ -178,12 +219,17 @@ lp_status lp_modes_combine(const lp_cfloat* modes, int n_modes, int nb, const do
                            lp_cfloat* field, int n, void* stream) {
   lp_status s = check_common(modes, n_modes, nb, field, n, coeffs);
   if (s != LP_OK) return s;
-  const size_t total = (size_t)n * n;
-  const size_t blocks = (total + kThreads - 1) / kThreads;
-  const int grid = (int)(blocks < 65535u * 16u ? blocks : 65535u * 16u);
-  combine_kernel<<<grid, kThreads, 0, (cudaStream_t)stream>>>(
-      reinterpret_cast<const float2*>(modes), n_modes, (long long)nb * nb, nb, coeffs,
-      reinterpret_cast<float2*>(field), n, (n - nb) / 2);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (nb < n) {  // zero the field outside the window
+    cudaError_t e = cudaMemsetAsync(field, 0, sizeof(lp_cfloat) * (size_t)n * n, st);
+    if (e != cudaSuccess) return fail(LP_ERR_CUDA, cudaGetErrorString(e));
+  }
+  const long long P = (long long)nb * nb;
+  const long long blocks = (P + kThreads - 1) / kThreads;
+  const int grid = (int)(blocks < 65535LL * 16 ? blocks : 65535LL * 16);
+  combine_kernel<<<grid, kThreads, 0, st>>>(reinterpret_cast<const float2*>(modes), n_modes, P,
+                                            nb, coeffs, reinterpret_cast<float2*>(field), n,
+                                            (n - nb) / 2);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LP_OK : fail(LP_ERR_CUDA, cudaGetErrorString(e));
 }

@@ -39,7 +39,7 @@ def test_deconstruct_construct_match_reference(lp, golden):
     assert rel(b.spectrum.cpu().numpy(), golden["modes_constructed_spectrum"]) < 1e-5
 
 
-@pytest.mark.parametrize("n,nb,M", [(512, 512, 40), (1024, 512, 64), (256, 64, 1000)])
+@pytest.mark.parametrize("n,nb,M", [(512, 512, 40), (1024, 512, 64), (256, 64, 1000), (300, 98, 13)])
 def test_project_combine_vs_oracle(lp, n, nb, M):
     from lightprop2d_gb300 import modes as MD
     rng = np.random.default_rng(n + M)
