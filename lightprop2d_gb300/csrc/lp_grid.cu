@@ -20,20 +20,49 @@ lp_status fail(lp_status s, const char* msg) { return (lp_status)set_last_error(
 
 bool aligned8(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 7u) == 0; }
 
+// CTAs for kernels that loop over output rows: per_sm per SM, at most one
+// per row (the crop kernel's per-CTA column table is amortised over the CTA's
+// rows, so it takes fewer CTAs than the plain copy).
+int g_sms_grid = 0;
+int rows_grid(int rows, int per_sm) {
+  if (!g_sms_grid) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sms_grid, cudaDevAttrMultiProcessorCount, dev);
+    if (g_sms_grid <= 0) g_sms_grid = 1;
+  }
+  const int g = per_sm * g_sms_grid;
+  return rows < g ? rows : g;
+}
+
 int grid_for(size_t points) {
   const size_t g = (points + kThreads - 1) / kThreads;
   return (int)(g < 65535u * 64u ? g : 65535u * 64u);
 }
 
-// out[y][x] = in[clamp(y - d)][clamp(x - d)] (beam2d.py:386-402).
-__global__ void expand_kernel(const float2* __restrict__ in, int n_in, float2* __restrict__ out,
-                              int n_out, int d) {
-  const size_t total = (size_t)n_out * n_out;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
-       i += (size_t)gridDim.x * blockDim.x) {
-    const int y = (int)(i / n_out), x = (int)(i % n_out);
-    const int sy = min(max(y - d, 0), n_in - 1), sx = min(max(x - d, 0), n_in - 1);
-    out[i] = in[(size_t)sy * n_in + sx];
+// out[y][x] = in[clamp(y - d)][clamp(x - d)] (beam2d.py:386-402).  A CTA
+// copies whole output rows (rows blockIdx.x, += gridDim.x), four points per
+// thread in flight.
+__global__ void __launch_bounds__(kThreads) expand_kernel(const float2* __restrict__ in,
+                                                          int n_in, float2* __restrict__ out,
+                                                          int n_out, int d) {
+  for (int y = blockIdx.x; y < n_out; y += gridDim.x) {
+    const int sy = min(max(y - d, 0), n_in - 1);
+    const float2* src = in + (size_t)sy * n_in;
+    float2* dst = out + (size_t)y * n_out;
+    for (int x0 = threadIdx.x; x0 < n_out; x0 += 4 * kThreads) {
+      float2 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int x = x0 + u * kThreads;
+        v[u] = x < n_out ? __ldg(src + min(max(x - d, 0), n_in - 1)) : make_float2(0.0f, 0.0f);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int x = x0 + u * kThreads;
+        if (x < n_out) dst[x] = v[u];
+      }
+    }
   }
 }
 
@@ -145,8 +174,7 @@ lp_status lp_expand(const lp_cfloat* in, int n_in, lp_cfloat* out, int n_out, vo
     return fail(LP_ERR_INVALID_ARGUMENT, "lp_expand: need n_out >= n_in with an even difference");
   if ((const void*)in == (const void*)out && n_out != n_in)
     return fail(LP_ERR_INVALID_ARGUMENT, "lp_expand: in and out must be different grids");
-  const size_t total = (size_t)n_out * n_out;
-  expand_kernel<<<grid_for(total), kThreads, 0, (cudaStream_t)stream>>>(
+  expand_kernel<<<rows_grid(n_out, 8), kThreads, 0, (cudaStream_t)stream>>>(
       reinterpret_cast<const float2*>(in), n_in, reinterpret_cast<float2*>(out), n_out,
       (n_out - n_in) / 2);
   return launch_check("lp_expand");
@@ -178,7 +206,7 @@ lp_status lp_crop(const lp_cfloat* in, int n_in, int first, int n_keep, double x
   if (n_out > kMaxOut) return fail(LP_ERR_UNSUPPORTED_SIZE, "lp_crop: n_out <= 4096");
   const FF r = ff_from_double(dL_out / dL_in);
   const FF o = ff_from_double(x0 / dL_in);
-  crop_kernel<<<n_out < 2048 ? n_out : 2048, kThreads, 0, (cudaStream_t)stream>>>(
+  crop_kernel<<<rows_grid(n_out, 4), kThreads, 0, (cudaStream_t)stream>>>(
       reinterpret_cast<const float2*>(in), n_in, first, n_keep, reinterpret_cast<float2*>(out),
       n_out, r.hi, r.lo, o.hi, o.lo);
   return launch_check("lp_crop");

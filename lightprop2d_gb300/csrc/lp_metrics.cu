@@ -20,16 +20,32 @@
 
 namespace {
 
-// One 1024-thread CTA per SM with 8 loads in flight per thread keeps ~10 MB
-// in flight on GB300; few CTAs keep the final FP64 atomics (3 per CTA onto
-// the same 40 bytes) from contending.
+// One 1024-thread CTA per SM with 16 loads in flight per thread keeps ~20 MB
+// in flight on GB300 (a 2048^2 grid in two round trips); few CTAs keep the
+// final FP64 atomics (3 per CTA onto the same 40 bytes) from contending.
 constexpr int kThreads = 1024;
-constexpr int kUnroll = 8;  // loads in flight per thread
+constexpr int kUnroll = 16;  // loads in flight per thread
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   return v;
+}
+
+// v[u] = f[i0 + u*stride] (0 past n2), all kUnroll loads issued before any
+// is used.
+__device__ __forceinline__ void load_block(float2 (&v)[kUnroll], const float2* __restrict__ f,
+                                           int i0, int stride, int n2) {
+  if (i0 + (kUnroll - 1) * stride < n2) {
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) v[u] = __ldg(f + i0 + u * stride);
+  } else {
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u) {
+      const int i = i0 + u * stride;
+      v[u] = i < n2 ? __ldg(f + i) : make_float2(0.0f, 0.0f);
+    }
+  }
 }
 
 // Adds v[0..K) over the CTA into out[0..K) (one atomicAdd per value per CTA).
@@ -53,59 +69,64 @@ __device__ __forceinline__ void cta_add(const float (&v)[K], double* out) {
   }
 }
 
+// The launch makes the grid stride (gridDim.x * kThreads points) a multiple
+// of n, so a thread's points all lie in one column: its jx is a constant
+// (sum jx I = jx * sum I) and jy advances by stride / n rows per step.
 __global__ void __launch_bounds__(kThreads) moments1_kernel(const float2* __restrict__ f,
                                                             int logn, double* out) {
+  // let the second pass's CTAs be scheduled as this pass's CTAs retire
+  asm volatile("griddepcontrol.launch_dependents;");
   const int n = 1 << logn, h = n >> 1;
-  const size_t n2 = (size_t)n * n;
-  float s[3] = {0.0f, 0.0f, 0.0f};
-  const size_t stride = (size_t)gridDim.x * kThreads;
-  for (size_t i0 = blockIdx.x * (size_t)kThreads + threadIdx.x; i0 < n2; i0 += kUnroll * stride) {
+  const int n2 = n * n;
+  const int stride = (int)gridDim.x * kThreads;
+  const int first = (int)blockIdx.x * kThreads + (int)threadIdx.x;
+  const float jx = (float)((first & (n - 1)) - h);
+  const float djy = (float)(stride >> logn);
+  float jy = (float)((first >> logn) - h);
+  float s0 = 0.0f, s2 = 0.0f;
+  for (int i0 = first; i0 < n2; i0 += kUnroll * stride) {
     float2 v[kUnroll];
-#pragma unroll
-    for (int u = 0; u < kUnroll; ++u) {  // independent loads in flight
-      const size_t i = i0 + u * stride;
-      v[u] = i < n2 ? __ldg(f + i) : make_float2(0.0f, 0.0f);
-    }
+    load_block(v, f, i0, stride, n2);
 #pragma unroll
     for (int u = 0; u < kUnroll; ++u) {
-      const size_t i = i0 + u * stride;
       const float I = fmaf(v[u].x, v[u].x, v[u].y * v[u].y);
-      const float jx = (float)((int)(i & (size_t)(n - 1)) - h);
-      const float jy = (float)((int)(i >> logn) - h);
-      s[0] += I;
-      s[1] = fmaf(jx, I, s[1]);
-      s[2] = fmaf(jy, I, s[2]);
+      s0 += I;
+      s2 = fmaf(fmaf((float)u, djy, jy), I, s2);
     }
+    jy = fmaf((float)kUnroll, djy, jy);
   }
+  const float s[3] = {s0, jx * s0, s2};
   cta_add<3>(s, out);
 }
 
 __global__ void __launch_bounds__(kThreads) moments2_kernel(const float2* __restrict__ f,
                                                             int logn, double* out) {
   const int n = 1 << logn, h = n >> 1;
-  const size_t n2 = (size_t)n * n;
+  const int n2 = n * n;
+  const int stride = (int)gridDim.x * kThreads;
+  const int first = (int)blockIdx.x * kThreads + (int)threadIdx.x;
+  // launched with programmatic dependent launch: wait for pass 1's sums
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const double m0 = out[0];
   const float xc = m0 > 0.0 ? (float)(out[1] / m0) : 0.0f;
   const float yc = m0 > 0.0 ? (float)(out[2] / m0) : 0.0f;
-  float s[2] = {0.0f, 0.0f};
-  const size_t stride = (size_t)gridDim.x * kThreads;
-  for (size_t i0 = blockIdx.x * (size_t)kThreads + threadIdx.x; i0 < n2; i0 += kUnroll * stride) {
+  const float dx = (float)((first & (n - 1)) - h) - xc;
+  const float ddy = (float)(stride >> logn);
+  float dy = (float)((first >> logn) - h) - yc;
+  float s0 = 0.0f, s1 = 0.0f;
+  for (int i0 = first; i0 < n2; i0 += kUnroll * stride) {
     float2 v[kUnroll];
+    load_block(v, f, i0, stride, n2);
 #pragma unroll
     for (int u = 0; u < kUnroll; ++u) {
-      const size_t i = i0 + u * stride;
-      v[u] = i < n2 ? __ldg(f + i) : make_float2(0.0f, 0.0f);
-    }
-#pragma unroll
-    for (int u = 0; u < kUnroll; ++u) {
-      const size_t i = i0 + u * stride;
       const float I = fmaf(v[u].x, v[u].x, v[u].y * v[u].y);
-      const float dx = (float)((int)(i & (size_t)(n - 1)) - h) - xc;
-      const float dy = (float)((int)(i >> logn) - h) - yc;
-      s[0] = fmaf(dx * dx, I, s[0]);
-      s[1] = fmaf(dy * dy, I, s[1]);
+      const float d = fmaf((float)u, ddy, dy);
+      s0 += I;
+      s1 = fmaf(d * d, I, s1);
     }
+    dy = fmaf((float)kUnroll, ddy, dy);
   }
+  const float s[2] = {dx * dx * s0, s1};
   cta_add<2>(s, out + 3);
 }
 
@@ -131,10 +152,15 @@ extern "C" lp_status lp_beam_moments(const lp_cfloat* field, int n, double* mome
   }
   int logn = 0;
   while ((1 << logn) < n) ++logn;
-  const size_t n2 = (size_t)n * n;
-  const size_t want = (n2 + kThreads * kUnroll - 1) / (kThreads * kUnroll);
-  const int grid = (int)(want < (size_t)g_sms_metrics ? (want ? want : 1)
-                                                      : (size_t)g_sms_metrics);
+  // grid: about one CTA per SM (fewer for small grids), a multiple of
+  // mult = n / 1024 when n > 1024 so that the stride (grid * 1024 points) is
+  // a multiple of n.
+  const int n2 = n * n;
+  const int want = (n2 + kThreads * kUnroll - 1) / (kThreads * kUnroll);
+  const int mult = n > kThreads ? n / kThreads : 1;
+  int grid = want < g_sms_metrics ? want : g_sms_metrics;
+  grid = grid / mult * mult;
+  if (grid < mult) grid = mult;
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e = cudaMemsetAsync(moments, 0, 5 * sizeof(double), st);
   if (e == cudaSuccess) {
@@ -143,9 +169,17 @@ extern "C" lp_status lp_beam_moments(const lp_cfloat* field, int n, double* mome
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
-    moments2_kernel<<<grid, kThreads, 0, st>>>(reinterpret_cast<const float2*>(field), logn,
-                                               moments);
-    e = cudaGetLastError();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kThreads);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, moments2_kernel, reinterpret_cast<const float2*>(field), logn,
+                           moments);
   }
   if (e != cudaSuccess)
     return (lp_status)set_last_error(LP_ERR_CUDA, cudaGetErrorString(e));
