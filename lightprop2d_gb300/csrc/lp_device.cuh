@@ -317,6 +317,27 @@ __device__ __forceinline__ float2 cis_cycles(float f, float sign) {
   return make_float2(c, sign * s);
 }
 
+// exp(i*phi) for an FP32 phase mask value in radians.  phi is first reduced
+// to [-pi, pi] by Cody-Waite reduction (k = rint(phi / 2pi), r = phi - k*2pi
+// with 2pi split into two floats, hi = fl(2pi) and lo = fl(2pi - hi); the
+// FMA keeps r to ~1 ulp for |phi| < 2^22), then the special-function unit's
+// sine/cosine (absolute error ~4e-7 on [-pi, pi]), a few instructions where
+// the accurate sincosf takes tens.  LP_ACCURATE_SINCOS selects sincosf.
+__device__ __forceinline__ float2 cis_radians(float phi) {
+  float s, c;
+#ifdef LP_ACCURATE_SINCOS
+  sincosf(phi, &s, &c);
+#else
+  constexpr float kInv2Pi = 0.15915493667125702f;
+  constexpr float k2PiHi = 6.2831854820251465f;
+  constexpr float k2PiLo = -1.7484555314695172e-07f;
+  const float k = rintf(phi * kInv2Pi);
+  const float r = fmaf(-k, k2PiLo, fmaf(-k, k2PiHi, phi));
+  __sincosf(r, &s, &c);
+#endif
+  return make_float2(c, s);
+}
+
 // Lens phase in cycles at integer offsets (jx, jy) from the grid centre:
 // (X^2+Y^2)*k0/(2f) radians = kappa*(jx^2+jy^2) cycles, kappa = dL^2 k0/(4 pi f).
 __device__ __forceinline__ float lens_cycles(float kap_hi, float kap_lo, float m) {

@@ -231,7 +231,8 @@ __device__ __forceinline__ void conj16(float2 (&v)[16]) {
 // in flight); real masks ignore `conj`.
 template <int N>
 __device__ __forceinline__ void apply_mask_row(float2 (&v)[16], const void* mask, int type,
-                                               int conj, int y, int t) {
+                                               int conj, int y, int t, float2* slots,
+                                               int nthreads, int tid) {
   constexpr int T = FftGeo<N>::T;
   const size_t row = (size_t)y * N + t;
   switch (type) {
@@ -260,12 +261,18 @@ __device__ __forceinline__ void apply_mask_row(float2 (&v)[16], const void* mask
     }
     case 4: {  // float32 phase: exp(i*phi)
       const float* p = reinterpret_cast<const float*>(mask) + row;
-      float ph[16];
-      static_for<16>([&](auto jc) { ph[jc.value] = __ldg(p + T * jc.value); });
+      static_for<16>([&](auto jc) { slots[jc.value * nthreads + tid].x = __ldg(p + T * jc.value); });
+#pragma unroll 1
+      for (int j0 = 0; j0 < 16; j0 += 4) {  // four independent evaluations in flight
+        float ph[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) ph[u] = slots[(j0 + u) * nthreads + tid].x;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) slots[(j0 + u) * nthreads + tid] = cis_radians(ph[u]);
+      }
       static_for<16>([&](auto jc) {
-        float sn, cs;
-        sincosf(ph[jc.value], &sn, &cs);
-        v[jc.value] = cmul(v[jc.value], make_float2(cs, conj ? -sn : sn));
+        const float2 m = slots[jc.value * nthreads + tid];
+        v[jc.value] = cmul(v[jc.value], conj ? cconj(m) : m);
       });
       break;
     }
@@ -326,7 +333,7 @@ __device__ __forceinline__ void apply_xops(float2 (&v)[16], float2* slots, int n
       v[j] = cmul(v[j], slots[j * nthreads + tid]);
     });
   }
-  if (ops.xmask) apply_mask_row<N>(v, ops.xmask, ops.xmask_type, ops.conj, y, t);
+  if (ops.xmask) apply_mask_row<N>(v, ops.xmask, ops.xmask_type, ops.conj, y, t, slots, nthreads, tid);
 }
 
 template <int N, bool CG = false>

@@ -48,7 +48,7 @@ def test_metrics_match_reference(lp, golden):
     check_metrics(metrics(M), golden["met_off_prop"], M.dL)
 
 
-@pytest.mark.parametrize("n", [64, 1024, 4096])
+@pytest.mark.parametrize("n", [16, 64, 1024, 2048, 4096])
 def test_metrics_vs_oracle_off_centre(lp, n):
     area = 2 * mm
     g = O.grids(area, n, 632 * nm)
@@ -86,6 +86,17 @@ def test_expand_coarse_match_reference(lp, golden):
     g = O.grids(2 * mm, 128, 632 * nm)
     _, ref = O.propagate(np.fft.fft2(golden["grid_coarse_field"]), g["Kz"], 0.5)
     assert O.rel_l2(H(G.field), ref) < 1e-5
+
+
+@pytest.mark.parametrize("n_in,n_out", [(1, 3), (100, 300), (2048, 4096), (64, 64)])
+def test_expand_kernel_edge_padding(lp, n_in, n_out):
+    """lp_expand is np.pad(mode="edge") exactly (beam2d.py:386-402), any size."""
+    from lightprop2d_gb300 import backend as B
+    rng = np.random.default_rng(n_in + n_out)
+    x = (rng.normal(size=(n_in, n_in)) + 1j * rng.normal(size=(n_in, n_in))).astype(np.complex64)
+    got = H(B.expand(torch.as_tensor(x, device="cuda"), n_out))
+    d = (n_out - n_in) // 2
+    assert np.array_equal(got, np.pad(x, d, mode="edge"))
 
 
 @pytest.mark.parametrize("n,area_out,n_out", [(256, 0.5, 128), (256, 0.6, 0), (1024, 0.3, 512)])
