@@ -145,6 +145,28 @@ def test_plain_matches_fused(B):
     assert O.rel_l2(host(fu), f_ref) < TOL
 
 
+@pytest.mark.parametrize("n", [256, 2048, 4096])
+def test_phase_mask_large_phases(B, n):
+    """An FP32 phase mask far outside [-pi, pi] (|phi| up to 800 rad) in the
+    first pass (register and TMA row kernels) and, with XMASK_AFTER, on the
+    store side of the last pass, against exp(1j*phi) in float64."""
+    from lightprop2d_gb300 import _lib as L
+    area, wl, z = 1 * mm, 632 * nm, 0.5
+    rng = np.random.default_rng(n + 5)
+    x = O.random_phase_hole(n, area, 0.3 * area, seed=n + 7)
+    phi = rng.uniform(-800.0, 800.0, (n, n)).astype(np.float32)
+    pm = torch.as_tensor(phi, device="cuda")
+    mult = np.exp(1j * phi.astype(np.float64))
+    g = O.grids(area, n, wl)
+    _, ref = O.propagate(np.fft.fft2(x * mult), g["Kz"], z)
+    got = host(B.propagate_field(dev(x), area, wl, z, xmask=pm, xmask_phase=True))
+    assert O.rel_l2(got, ref) < TOL
+    _, ref2 = O.propagate(np.fft.fft2(x), g["Kz"], z)
+    got2 = host(B.propagate_field(dev(x), area, wl, z, xmask=pm, xmask_phase=True,
+                                  flags=L.LP_FLAG_XMASK_AFTER))
+    assert O.rel_l2(got2, ref2 * mult) < TOL
+
+
 def test_adjoint_identity(B):
     """<P u, v> == <u, P^H v> for the fused operator with lens and masks."""
     from lightprop2d_gb300 import _lib as L
