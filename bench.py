@@ -77,12 +77,14 @@ def _cpu_worker_step(z):
     return dt, float(_np.abs(out[0, 0]))
 
 
-def cpu_baseline(steps: int, n=N_HEAD, procs=None):
-    """Run `steps` rounds; each round every process propagates one beam."""
+def cpu_baseline(steps: int, n=N_HEAD, procs=None, warmup=3):
+    """Run `warmup` untimed then `steps` timed rounds; each round every
+    process propagates one beam."""
     procs = procs or os.cpu_count() or 1
     ctx = mp.get_context("spawn")
     with ctx.Pool(procs, initializer=_cpu_worker_init, initargs=(n, AREA, WL)) as pool:
-        pool.map(_cpu_worker_step, [Z] * procs)  # warm-up
+        for _ in range(max(1, warmup)):
+            pool.map(_cpu_worker_step, [Z] * procs)
         walls = []
         for _ in range(steps):
             t0 = time.perf_counter()
@@ -98,11 +100,14 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
+    # bounded sample: at most 10 timed and 5 warm-up rounds (a round is one
+    # 2048^2 propagate per host core, ~0.2-0.9 s)
     steps = max(1, min(args.steps, 10))
-    cb = cpu_baseline(steps)
+    warmup = max(3, min(args.warmup, 5))
+    cb = cpu_baseline(steps, warmup=warmup)
     line = {
         "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
-        "n_gpus": args.gpus, "steps": steps, "warmup": 1,
+        "n_gpus": args.gpus, "steps": steps, "warmup": warmup,
         "ms_per_step": 1000.0 / cb["value"] * cb["cores"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "flush_l2": False},
