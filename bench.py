@@ -655,6 +655,19 @@ def main():
                 return 0
             cu, _ = timed(cufft_plain, ks, 3)
             del Hc
+            # the reference's own sequence on the GPU (what its CuPy path runs):
+            # cuFFT fft2, H = exp(2*pi*i*(trunc(Kz z) - Kz z)) built in FP64 from a
+            # cached FP64 Kz grid every call (beam2d.py:485-489), multiply, ifft2
+            Kz_d = torch.as_tensor(g["Kz"], device=dev)
+
+            def cufft_fp64h(i):
+                fi, fo = slots[i % R]
+                dk = Kz_d * Z
+                h = torch.polar(torch.ones_like(dk), 2 * np.pi * (torch.trunc(dk) - dk))
+                fo.copy_(torch.fft.ifft2(torch.fft.fft2(fi) * h.to(torch.complex64)))
+                return 0
+            cu64, _ = timed(cufft_fp64h, max(5, ks // 4), 3)
+            del Kz_d
         del specs
         torch.cuda.synchronize()
         # FP32-phase vs float-float phase error at every z of the workload
@@ -689,6 +702,12 @@ def main():
                               "fused_speedup": round(statistics.fmean(pl) / ms_step, 3)},
             "plain_unfused_fp64_h": {"ms": round(statistics.fmean(pl64), 5),
                                      "fused_speedup": round(statistics.fmean(pl64) / ms_step, 3)},
+            "cufft_fp64_h_reference_sequence": {
+                "ms": round(statistics.fmean(cu64), 5),
+                "fused_speedup": round(statistics.fmean(cu64) / ms_step, 3),
+                "note": "the reference's propagate sequence on the GPU: torch.fft fft2, FP64 H "
+                        "from a cached FP64 Kz grid every call, multiply, ifft2; not part of "
+                        "the product"},
             "cufft_plain_reference_point": {
                 "ms": round(statistics.fmean(cu), 5),
                 "fused_speedup": round(statistics.fmean(cu) / ms_step, 3),
