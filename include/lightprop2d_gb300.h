@@ -189,6 +189,18 @@ lp_status lp_iprofile(const lp_cfloat* field, float* out, int n, void* stream);
  * so Xc = dL*[1]/[0], D4sigma_x = 4*dL*sqrt([3]/[0]).  Two read-only passes
  * (the second moments about the centroid, like the reference); asynchronous. */
 lp_status lp_beam_moments(const lp_cfloat* field, int n, double* moments, void* stream);
+/* Intensity loss of the differentiable design workload (no reference
+ * counterpart: the inverse-design loop built on propagate, beam2d.py:462-490).
+ * Forward: *loss_sum = sum_i (|y_i|^2 - target_i)^2 over `count` points, in
+ * FP64 (device memory, overwritten).  Backward (lp_intensity_mse_grad):
+ * grad_y_i = (*upstream) * scale * (|y_i|^2 - target_i) * y_i, with `upstream`
+ * a device float (the incoming gradient, read on the device so the call can
+ * be captured in a CUDA graph) and scale = 4 / count for the mean. */
+lp_status lp_intensity_mse(const lp_cfloat* y, const float* target, long long count,
+                           double* loss_sum, void* stream);
+lp_status lp_intensity_mse_grad(const lp_cfloat* y, const float* target, long long count,
+                                const float* upstream, float scale, lp_cfloat* grad_y,
+                                void* stream);
 
 /* spectrum *= H(z) only (no transform): used to materialise a spectrum whose
  * propagation distance the caller kept pending. */

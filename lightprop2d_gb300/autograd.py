@@ -76,6 +76,32 @@ class _Propagate(torch.autograd.Function):
         return (grad_u if need_u else None), grad_phi, grad_z, None, None, None, None, None
 
 
+class _IntensityMSE(torch.autograd.Function):
+    """mean((|y|^2 - target)^2) in one reduction kernel; its gradient
+    4/count * (|y|^2 - target) * y in one elementwise kernel (the upstream
+    gradient is read on the device, so the step stays graph-capturable)."""
+
+    @staticmethod
+    def forward(ctx, y, target):
+        ctx.save_for_backward(y, target)
+        s = B.intensity_mse_sum(y, target)
+        return (s / y.numel()).to(torch.float32).reshape(())
+
+    @staticmethod
+    def backward(ctx, g):
+        y, target = ctx.saved_tensors
+        up = g.reshape(1).to(torch.float32).contiguous()
+        return B.intensity_mse_grad(y, target, up, 4.0 / y.numel()), None
+
+
+def intensity_mse(y: torch.Tensor, target: torch.Tensor) -> torch.Tensor:
+    """Differentiable mean((|y|^2 - target)^2) for complex64 y and float32
+    target of the same shape (library kernels for the value and gradient)."""
+    if y.dtype != torch.complex64:
+        raise ValueError("y must be complex64")
+    return _IntensityMSE.apply(y.contiguous(), target.to(torch.float32).contiguous())
+
+
 def propagate(field: torch.Tensor, z, area_size: float, wl: float, phase=None,
               lens_f: float = 0.0, kmask=None, phase_after: bool = False) -> torch.Tensor:
     """Differentiable fused propagate (field, phase mask and z gradients).

@@ -205,6 +205,35 @@ def beam_moments(field: torch.Tensor, out: torch.Tensor | None = None) -> torch.
     return out
 
 
+def intensity_mse_sum(y: torch.Tensor, target: torch.Tensor,
+                      out: torch.Tensor | None = None) -> torch.Tensor:
+    """sum (|y|^2 - target)^2 as one float64 on the device (lp_intensity_mse)."""
+    _check_loss_args(y, target)
+    out = torch.empty(1, dtype=torch.float64, device=y.device) if out is None else out
+    _call("lp_intensity_mse", y.device, _vp(y), _vp(target), y.numel(), _vp(out))
+    return out
+
+
+def intensity_mse_grad(y: torch.Tensor, target: torch.Tensor, upstream: torch.Tensor,
+                       scale: float, out: torch.Tensor | None = None) -> torch.Tensor:
+    """upstream * scale * (|y|^2 - target) * y (lp_intensity_mse_grad); upstream
+    is a one-element float32 CUDA tensor read on the device."""
+    _check_loss_args(y, target)
+    if upstream.dtype != torch.float32 or not upstream.is_cuda or upstream.numel() != 1:
+        raise ValueError("upstream: one-element float32 CUDA tensor")
+    out = torch.empty_like(y) if out is None else out
+    _call("lp_intensity_mse_grad", y.device, _vp(y), _vp(target), y.numel(),
+          _vp(upstream.contiguous()), float(scale), _vp(out))
+    return out
+
+
+def _check_loss_args(y: torch.Tensor, target: torch.Tensor) -> None:
+    if y.dtype != torch.complex64 or not y.is_cuda or not y.is_contiguous():
+        raise ValueError("y: contiguous complex64 CUDA tensor")
+    if target.dtype != torch.float32 or target.shape != y.shape or not target.is_contiguous():
+        raise ValueError("target: contiguous float32 tensor of y's shape")
+
+
 def expand(field: torch.Tensor, n_out: int) -> torch.Tensor:
     """Edge-replicated padding to n_out x n_out (lp_expand; beam2d.py:375-404)."""
     n = _grid(field, "field")

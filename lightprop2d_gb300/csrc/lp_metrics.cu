@@ -185,3 +185,115 @@ extern "C" lp_status lp_beam_moments(const lp_cfloat* field, int n, double* mome
     return (lp_status)set_last_error(LP_ERR_CUDA, cudaGetErrorString(e));
   return LP_OK;
 }
+
+// ------------------------------------------------------- intensity loss --
+namespace {
+
+constexpr int kLossThreads = 256;
+
+__global__ void __launch_bounds__(kLossThreads) mse_sum_kernel(const float2* __restrict__ y,
+                                                               const float* __restrict__ tg,
+                                                               long long count, double* out) {
+  float s = 0.0f;
+  const long long stride = (long long)gridDim.x * kLossThreads;
+  for (long long i = (long long)blockIdx.x * kLossThreads + threadIdx.x; i < count;
+       i += 4 * stride) {
+    float2 v[4];
+    float t[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {  // four independent loads in flight
+      const long long k = i + u * stride;
+      v[u] = k < count ? __ldg(y + k) : make_float2(0.0f, 0.0f);
+      t[u] = k < count ? __ldg(tg + k) : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const float d = fmaf(v[u].x, v[u].x, fmaf(v[u].y, v[u].y, -t[u]));
+      s = fmaf(d, d, s);
+    }
+  }
+  __shared__ double part[kLossThreads / 32];
+  double a = warp_sum((double)s);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    a = threadIdx.x < kLossThreads / 32 ? part[threadIdx.x] : 0.0;
+    a = warp_sum(a);
+    if (threadIdx.x == 0) atomicAdd(out, a);
+  }
+}
+
+__global__ void __launch_bounds__(kLossThreads) mse_grad_kernel(
+    const float2* __restrict__ y, const float* __restrict__ tg, long long count,
+    const float* __restrict__ upstream, float scale, float2* __restrict__ g) {
+  const float c = scale * __ldg(upstream);
+  for (long long i = (long long)blockIdx.x * kLossThreads + threadIdx.x; i < count;
+       i += (long long)gridDim.x * kLossThreads) {
+    const float2 v = __ldg(y + i);
+    const float d = fmaf(v.x, v.x, fmaf(v.y, v.y, -__ldg(tg + i))) * c;
+    g[i] = make_float2(d * v.x, d * v.y);
+  }
+}
+
+int loss_grid(long long count, int per_thread) {
+  const long long want = (count + (long long)kLossThreads * per_thread - 1) /
+                         ((long long)kLossThreads * per_thread);
+  const long long cap = 8LL * (g_sms_metrics > 0 ? g_sms_metrics : 1);
+  return (int)(want < 1 ? 1 : want < cap ? want : cap);
+}
+
+lp_status loss_args(const void* y, const void* target, long long count, const void* out) {
+  using namespace lp;
+  if (!y || !target || !out)
+    return (lp_status)set_last_error(LP_ERR_INVALID_ARGUMENT, "intensity loss: NULL pointer");
+  if (count < 1)
+    return (lp_status)set_last_error(LP_ERR_INVALID_ARGUMENT, "intensity loss: count >= 1");
+  if ((reinterpret_cast<uintptr_t>(y) & 7u) || (reinterpret_cast<uintptr_t>(target) & 3u) ||
+      (reinterpret_cast<uintptr_t>(out) & 3u))
+    return (lp_status)set_last_error(LP_ERR_MISALIGNED, "intensity loss: alignment");
+  if (!g_sms_metrics) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sms_metrics, cudaDevAttrMultiProcessorCount, dev);
+    if (g_sms_metrics <= 0) g_sms_metrics = 1;
+  }
+  return LP_OK;
+}
+
+}  // namespace
+
+extern "C" lp_status lp_intensity_mse(const lp_cfloat* y, const float* target, long long count,
+                                      double* loss_sum, void* stream) {
+  using namespace lp;
+  lp_status s = loss_args(y, target, count, loss_sum);
+  if (s != LP_OK) return s;
+  if (reinterpret_cast<uintptr_t>(loss_sum) & 7u)
+    return (lp_status)set_last_error(LP_ERR_MISALIGNED, "lp_intensity_mse: loss_sum alignment");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaMemsetAsync(loss_sum, 0, sizeof(double), st);
+  if (e == cudaSuccess) {
+    mse_sum_kernel<<<loss_grid(count, 4), kLossThreads, 0, st>>>(
+        reinterpret_cast<const float2*>(y), target, count, loss_sum);
+    e = cudaGetLastError();
+  }
+  return e == cudaSuccess ? LP_OK
+                          : (lp_status)set_last_error(LP_ERR_CUDA, cudaGetErrorString(e));
+}
+
+extern "C" lp_status lp_intensity_mse_grad(const lp_cfloat* y, const float* target,
+                                           long long count, const float* upstream, float scale,
+                                           lp_cfloat* grad_y, void* stream) {
+  using namespace lp;
+  lp_status s = loss_args(y, target, count, grad_y);
+  if (s != LP_OK) return s;
+  if (!upstream || (reinterpret_cast<uintptr_t>(upstream) & 3u) ||
+      (reinterpret_cast<uintptr_t>(grad_y) & 7u))
+    return (lp_status)set_last_error(LP_ERR_INVALID_ARGUMENT,
+                                     "lp_intensity_mse_grad: upstream / grad_y pointer");
+  mse_grad_kernel<<<loss_grid(count, 1), kLossThreads, 0, (cudaStream_t)stream>>>(
+      reinterpret_cast<const float2*>(y), target, count, upstream, scale,
+      reinterpret_cast<float2*>(grad_y));
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LP_OK
+                          : (lp_status)set_last_error(LP_ERR_CUDA, cudaGetErrorString(e));
+}

@@ -72,8 +72,7 @@ def design_phase_mask(n=1024, area=0.1, wl=1064e-7, waist=300e-4, z=10.0, steps=
 
     def step():
         out = A.propagate(field, z, area, wl, phase=phase)
-        inten = out.real ** 2 + out.imag ** 2
-        loss = ((inten - target) ** 2).mean()
+        loss = A.intensity_mse(out, target)    # mean((|out|^2 - target)^2)
         loss.backward()
         opt.step()
         return loss.detach()

@@ -171,6 +171,27 @@ def test_inverse_design_reduces_loss():
     assert losses[-1] < 0.7 * losses[0]
 
 
+def test_intensity_mse_matches_torch():
+    """The fused loss kernel and its gradient against the same loss written
+    in torch (float64 reference)."""
+    from lightprop2d_gb300 import autograd as A
+    rng = np.random.default_rng(7)
+    for n in (64, 1024):
+        y0 = (rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))).astype(np.complex64)
+        t = rng.uniform(0, 2, (n, n)).astype(np.float32)
+        y = torch.as_tensor(y0, device="cuda").requires_grad_(True)
+        tt = torch.as_tensor(t, device="cuda")
+        loss = A.intensity_mse(y, tt)
+        (3.0 * loss).backward()
+        yr = torch.as_tensor(y0.astype(np.complex128)).requires_grad_(True)
+        ref = ((yr.real ** 2 + yr.imag ** 2 - torch.as_tensor(t, dtype=torch.float64)) ** 2).mean()
+        (3.0 * ref).backward()
+        assert abs(float(loss) - float(ref)) <= 1e-6 * abs(float(ref))
+        g = y.grad.cpu().numpy()
+        gr = yr.grad.numpy()
+        assert np.linalg.norm(g - gr) <= 1e-5 * np.linalg.norm(gr)
+
+
 def test_inverse_design_graph_matches_eager():
     """The CUDA-graph training step replays the same computation as eager."""
     from lightprop2d_gb300 import design as D
