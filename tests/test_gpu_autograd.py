@@ -186,7 +186,7 @@ def test_intensity_mse_matches_torch():
         yr = torch.as_tensor(y0.astype(np.complex128)).requires_grad_(True)
         ref = ((yr.real ** 2 + yr.imag ** 2 - torch.as_tensor(t, dtype=torch.float64)) ** 2).mean()
         (3.0 * ref).backward()
-        assert abs(float(loss) - float(ref)) <= 1e-6 * abs(float(ref))
+        assert abs(float(loss.detach()) - float(ref.detach())) <= 1e-6 * abs(float(ref.detach()))
         g = y.grad.cpu().numpy()
         gr = yr.grad.numpy()
         assert np.linalg.norm(g - gr) <= 1e-5 * np.linalg.norm(gr)
