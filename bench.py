@@ -80,7 +80,8 @@ def _cpu_worker_step(z):
 def cpu_baseline(steps: int, n=N_HEAD, procs=None, warmup=3):
     """Run `warmup` untimed then `steps` timed rounds; each round every
     process propagates one beam."""
-    procs = procs or os.cpu_count() or 1
+    # LP_BENCH_CPU_PROCS caps the processes (default: one per host core)
+    procs = procs or int(os.environ.get("LP_BENCH_CPU_PROCS", "0")) or os.cpu_count() or 1
     ctx = mp.get_context("spawn")
     with ctx.Pool(procs, initializer=_cpu_worker_init, initargs=(n, AREA, WL)) as pool:
         for _ in range(max(1, warmup)):

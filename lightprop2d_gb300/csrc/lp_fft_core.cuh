@@ -28,12 +28,6 @@
 #include "lp_device.cuh"
 #include "lp_internal.h"
 
-// 1: stage twiddles of radix 8/16 stages from a factored subset of the table
-// (fewer shared-memory loads, one extra rounding on some twiddles).
-#ifndef LP_TW_FACTOR
-#define LP_TW_FACTOR 0
-#endif
-
 namespace lp {
 
 template <int N>
@@ -166,39 +160,12 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[16], float2* buf, const fl
     const int k = b & (NS - 1);
     float2 a[R];
     static_for<R>([&](auto rc) { a[decltype(rc)::value] = v[q + nb * decltype(rc)::value]; });
-#if LP_TW_FACTOR
-    // W^(r k), r = 4a + b: load W^(b k) (b < 4) and W^(4a k), and form the
-    // other products with one complex multiply each (R = 16: 6 shared-memory
-    // loads instead of 15; R = 8: 4 instead of 7).
-    if constexpr (R >= 8) {
-      float2 lo[4], hi[R / 4];
-      static_for<3>([&](auto bc) {
-        constexpr int b = decltype(bc)::value + 1;
-        lo[b] = tw[OFF + b * NS + k];
-        if constexpr (S > 0) lo[b].y = -lo[b].y;
-      });
-      static_for<R / 4 - 1>([&](auto ac) {
-        constexpr int c = decltype(ac)::value + 1;
-        hi[c] = tw[OFF + 4 * c * NS + k];
-        if constexpr (S > 0) hi[c].y = -hi[c].y;
-      });
-      static_for<R - 1>([&](auto rc) {
-        constexpr int r = decltype(rc)::value + 1;
-        constexpr int c = r / 4, b = r % 4;
-        if constexpr (c == 0) a[r] = cmul(a[r], lo[b]);
-        else if constexpr (b == 0) a[r] = cmul(a[r], hi[c]);
-        else a[r] = cmul(a[r], cmul(hi[c], lo[b]));
-      });
-    } else
-#endif
-    {
-      static_for<R - 1>([&](auto rc) {
-        constexpr int r = decltype(rc)::value + 1;
-        float2 w = tw[OFF + r * NS + k];
-        if constexpr (S > 0) w.y = -w.y;
-        a[r] = cmul(a[r], w);
-      });
-    }
+    static_for<R - 1>([&](auto rc) {
+      constexpr int r = decltype(rc)::value + 1;
+      float2 w = tw[OFF + r * NS + k];
+      if constexpr (S > 0) w.y = -w.y;
+      a[r] = cmul(a[r], w);
+    });
     Dft<R, S>::run(a);
     if constexpr (LAST) {
       static_for<R>([&](auto rc) { v[q + nb * decltype(rc)::value] = a[decltype(rc)::value]; });
