@@ -201,6 +201,13 @@ lp_status lp_intensity_mse(const lp_cfloat* y, const float* target, long long co
 lp_status lp_intensity_mse_grad(const lp_cfloat* y, const float* target, long long count,
                                 const float* upstream, float scale, lp_cfloat* grad_y,
                                 void* stream);
+/* Gradient of a real loss with respect to an FP32 phase mask phi applied as
+ * x -> x * exp(i*phi) (no reference counterpart: the backward of
+ * coordinate_filter with a phase, beam2d.py:310-342, in the differentiable
+ * workload): out_i = Im(conj(x_i) * g_i), with x the multiplied field and g
+ * the gradient with respect to it, over `count` points. */
+lp_status lp_phase_grad(const lp_cfloat* x, const lp_cfloat* g, long long count, float* out,
+                        void* stream);
 
 /* spectrum *= H(z) only (no transform): used to materialise a spectrum whose
  * propagation distance the caller kept pending. */

@@ -81,6 +81,7 @@ SIGNATURES = {
     "lp_beam_moments": [_vp, _i, _vp, _vp],
     "lp_intensity_mse": [_vp, _vp, ctypes.c_longlong, _vp, _vp],
     "lp_intensity_mse_grad": [_vp, _vp, ctypes.c_longlong, _vp, ctypes.c_float, _vp, _vp],
+    "lp_phase_grad": [_vp, _vp, ctypes.c_longlong, _vp, _vp],
     "lp_expand": [_vp, _i, _vp, _i, _vp],
     "lp_coarse": [_vp, _i, _vp, _i, _vp],
     "lp_crop": [_vp, _i, _i, _i, _d, _d, _vp, _i, _d, _vp],

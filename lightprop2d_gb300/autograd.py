@@ -65,8 +65,8 @@ class _Propagate(torch.autograd.Function):
             # Im(conj(x) * grad_x) at the multiplied field x:
             #   before propagation x = u*m, grad_x = conj(m)... -> Im(conj(u) grad_u)
             #   after propagation  x = y,   grad_x = grad_y
-            grad_phi = ((field.conj() * grad_u) if not after else (out.conj() * gy)).imag
-            grad_phi = grad_phi.to(phase.dtype)
+            grad_phi = (B.phase_grad(field.contiguous(), grad_u) if not after
+                        else B.phase_grad(out, gy))
         if need_z:
             dydz = B.propagate_field(field.contiguous(), area, wl, zv, lens_f=lens_f,
                                      xmask=phase, xmask_phase=has_phase, kmask=kmask,
@@ -156,7 +156,7 @@ class _Chain(torch.autograd.Function):
                 if need_phi:
                     y = states[k - k0 + 1] if k < k1 - 1 else (
                         ckpts[seg + 1] if seg + 1 < nseg else final)
-                    grad_screens[k] = (y.conj() * g).imag
+                    B.phase_grad(y, g, out=grad_screens[k])     # Im(conj(y) * g)
                 g = B.propagate_field(g, area, wl, dz, xmask=screens[k], xmask_phase=True,
                                       flags=L.LP_FLAG_ADJOINT | L.LP_FLAG_XMASK_AFTER)
             del states

@@ -227,6 +227,19 @@ def intensity_mse_grad(y: torch.Tensor, target: torch.Tensor, upstream: torch.Te
     return out
 
 
+def phase_grad(x: torch.Tensor, g: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+    """Im(conj(x) * g) as float32 (lp_phase_grad): the gradient of a real loss
+    with respect to a phase mask applied as x = u * exp(i*phi)."""
+    for t, nm in ((x, "x"), (g, "g")):
+        if t.dtype != torch.complex64 or not t.is_cuda or not t.is_contiguous():
+            raise ValueError(f"{nm}: contiguous complex64 CUDA tensor")
+    if g.shape != x.shape:
+        raise ValueError("g must have x's shape")
+    out = torch.empty(x.shape, dtype=torch.float32, device=x.device) if out is None else out
+    _call("lp_phase_grad", x.device, _vp(x), _vp(g), x.numel(), _vp(out))
+    return out
+
+
 def _check_loss_args(y: torch.Tensor, target: torch.Tensor) -> None:
     if y.dtype != torch.complex64 or not y.is_cuda or not y.is_contiguous():
         raise ValueError("y: contiguous complex64 CUDA tensor")

@@ -235,6 +235,16 @@ __global__ void __launch_bounds__(kLossThreads) mse_grad_kernel(
   }
 }
 
+__global__ void __launch_bounds__(kLossThreads) phase_grad_kernel(
+    const float2* __restrict__ x, const float2* __restrict__ g, long long count,
+    float* __restrict__ out) {
+  for (long long i = (long long)blockIdx.x * kLossThreads + threadIdx.x; i < count;
+       i += (long long)gridDim.x * kLossThreads) {
+    const float2 a = __ldg(x + i), b = __ldg(g + i);
+    out[i] = fmaf(a.x, b.y, -a.y * b.x);  // Im(conj(a) * b)
+  }
+}
+
 int loss_grid(long long count, int per_thread) {
   const long long want = (count + (long long)kLossThreads * per_thread - 1) /
                          ((long long)kLossThreads * per_thread);
@@ -293,6 +303,20 @@ extern "C" lp_status lp_intensity_mse_grad(const lp_cfloat* y, const float* targ
   mse_grad_kernel<<<loss_grid(count, 1), kLossThreads, 0, (cudaStream_t)stream>>>(
       reinterpret_cast<const float2*>(y), target, count, upstream, scale,
       reinterpret_cast<float2*>(grad_y));
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? LP_OK
+                          : (lp_status)set_last_error(LP_ERR_CUDA, cudaGetErrorString(e));
+}
+
+extern "C" lp_status lp_phase_grad(const lp_cfloat* x, const lp_cfloat* g, long long count,
+                                   float* out, void* stream) {
+  using namespace lp;
+  lp_status s = loss_args(x, out, count, out);
+  if (s != LP_OK) return s;
+  if (!g || (reinterpret_cast<uintptr_t>(g) & 7u))
+    return (lp_status)set_last_error(LP_ERR_INVALID_ARGUMENT, "lp_phase_grad: g pointer");
+  phase_grad_kernel<<<loss_grid(count, 1), kLossThreads, 0, (cudaStream_t)stream>>>(
+      reinterpret_cast<const float2*>(x), reinterpret_cast<const float2*>(g), count, out);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? LP_OK
                           : (lp_status)set_last_error(LP_ERR_CUDA, cudaGetErrorString(e));
