@@ -197,6 +197,22 @@ def gaussian(npoints, area_size, A0, rho0):
     return A0 * np.exp(-(g["X"] ** 2 + g["Y"] ** 2) / rho0 ** 2)
 
 
+def gaussian_paraxial(npoints, area_size, wl, rho0, z):
+    """Analytic paraxial propagation of ``gaussian(npoints, area_size, 1,
+    rho0)`` by z (the known answer of config 2 and of the reference's
+    tests/test_analytics.py:53-71): with k = 2*pi/wl, z_R = k*rho0^2/2,
+    q = z + i*z_R, E = (i*z_R/q) * exp(-i*k*r^2/(2q)) * exp(-i*k*z).  The
+    angular-spectrum result departs from it by the non-paraxial terms
+    (~2.5e-7 rel-L2 per cm at 2 mm / 2048^2 / 632 nm / 100 um) until the beam
+    wraps in the periodic window."""
+    g = grids(area_size, npoints, wl)
+    k = 2 * np.pi / wl
+    zr = k * rho0 ** 2 / 2
+    q0 = 1j * zr
+    q = q0 + z
+    return (q0 / q) * np.exp(-1j * k * (g["X"] ** 2 + g["Y"] ** 2) / (2 * q)) * np.exp(-1j * k * z)
+
+
 # --------------------------------------------------------------------------
 # Beam metrics and grid management (beam2d.py:375-460, :669-752).
 # --------------------------------------------------------------------------

@@ -132,6 +132,18 @@ def test_config2_gaussian_2048_all_z(B):
     assert errs_32[-1] > 10 * errs_ff[-1], (errs_32, errs_ff)
 
 
+def test_config2_vs_analytic_gaussian(B):
+    """The fused GPU propagate of config 2 against the analytic paraxial
+    Gaussian (z <= 10 cm; at 50 cm the beam wraps in the window): the
+    departure is the oracle's own non-paraxial term plus FP32 round-off."""
+    n, area, wl, w0 = 2048, 2 * mm, 632 * nm, 100 * um
+    f0 = O.gaussian(n, area, 1.0, w0)
+    for z in (0.1, 1.0, 5.0, 10.0):
+        f = host(B.propagate_field(dev(f0), area, wl, z))
+        e = O.rel_l2(f, O.gaussian_paraxial(n, area, wl, w0, z))
+        assert e < 3e-7 * z + 1e-6, (z, e)
+
+
 def test_plain_matches_fused(B):
     n, area, wl, z = 1024, 2 * mm, 632 * nm, 2.5
     g = O.grids(area, n, wl)

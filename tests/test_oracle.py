@@ -101,6 +101,19 @@ def test_mixed_sequence(golden):
     assert np.isclose(b.z, golden["mix_z"])
 
 
+def test_config2_oracle_vs_analytic_gaussian():
+    """2048^2, 2 mm, 632 nm, waist 100 um: the oracle's angular spectrum
+    against the analytic paraxial Gaussian at z = 0.1..10 cm (the departure
+    grows linearly with z: non-paraxial terms)."""
+    n, area, wl, w0 = 2048, 2 * mm, 632 * nm, 100 * um
+    g = O.grids(area, n, wl)
+    s0 = np.fft.fft2(O.gaussian(n, area, 1.0, w0))
+    for z in (0.1, 1.0, 5.0, 10.0):
+        _, f = O.propagate(s0, g["Kz"], z)
+        e = O.rel_l2(f, O.gaussian_paraxial(n, area, wl, w0, z))
+        assert e < 3e-7 * z, (z, e)
+
+
 @pytest.mark.parametrize("tag", ["a8", "a16"])
 def test_gaussian_known_answer(golden, tag):
     """On-axis intensity vs 1/(1+z_n^2) (tests/test_analytics.py:53-71)."""
