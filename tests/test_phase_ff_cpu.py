@@ -1,7 +1,9 @@
-"""CPU: the transfer-function phase arithmetic of the column pass, restated in
-numpy float32 operation by operation (column_constant + kz_phase_ff in
-lp_device.cuh, parameters as make_kparams in lp_capi.cu), against the
-float64 phase Kz*z of the reference (beam2d.py:485-489).
+"""CPU: the kernels' phase arithmetic restated in numpy float32 operation by
+operation -- the transfer-function phase of the column pass (column_constant
++ kz_phase_ff in lp_device.cuh, parameters as make_kparams in lp_capi.cu)
+against the float64 phase Kz*z of the reference (beam2d.py:485-489), the
+lens phase (lens_cycles, beam2d.py:508-511) and the reduction of FP32 phase
+masks (cis_radians).
 
 This pins the precision design without a GPU: the float-float phase stays
 within 6e-8 cycles of float64 out to z = 50 cm (the float32 rounding of the
@@ -125,3 +127,40 @@ def test_float_float_phase_near_cutoff(n, area, wl, z):
     assert max_err(f, evan, n, area, wl, z) < 1e-7
     g, evan0 = phase_ff(n, area, wl, z, renormalise=False)
     assert max_err(g, evan0, n, area, wl, z) > 10 * max_err(f, evan, n, area, wl, z)
+
+
+def test_lens_phase_float_float():
+    """Lens phase kappa*(jx^2+jy^2) cycles (lens_cycles, set_lens): exact
+    integer jx^2+jy^2, float-float kappa, against float64, at 2048^2, 2 mm,
+    632 nm and f = 1 cm (about 13 cycles at the corner: 79 rad at r = 1 mm)."""
+    n, area, wl, f = 2048, 0.2, 632e-7, 1.0
+    dl = area / n
+    kh, kl = ff(dl * dl * (1.0 / wl) / (4.0 * np.pi * f))
+    j = np.arange(n, dtype=np.int64) - n // 2
+    m64 = j[None, :] ** 2 + j[:, None] ** 2
+    m = m64.astype(f32)
+    assert np.array_equal(m.astype(np.int64), m64)                # exact integers
+    khf, klf = np.full(m.shape, kh, f32), np.full(m.shape, kl, f32)
+    c_hi, c_e = two_prod(khf, m)
+    c_lo = fma(klf, m, c_e)
+    got = ((c_hi - np.rint(c_hi)).astype(f32) + c_lo).astype(f32).astype(np.float64)
+    ref = m64 * (dl * dl * (1.0 / wl) / (4.0 * np.pi * f))
+    d = got - ref
+    d -= np.rint(d)
+    assert np.abs(d).max() < 6e-8
+
+
+def test_cody_waite_phase_reduction():
+    """cis_radians' reduction of an FP32 phase mask value to [-pi, pi]:
+    r = fma(-k, lo, fma(-k, hi, phi)), k = rint(phi / 2pi), 2pi = hi + lo,
+    stays within 2.5e-7 rad (about one ulp of pi) of the exact reduction for
+    |phi| up to 1e4 rad."""
+    rng = np.random.default_rng(3)
+    phi = rng.uniform(-1e4, 1e4, 200000).astype(f32)
+    hi, lo = ff(2 * np.pi)
+    inv = f32(1 / (2 * np.pi))
+    k = np.rint((phi * inv).astype(f32)).astype(f32)
+    r = fma(-k, np.full_like(k, lo), fma(-k, np.full_like(k, hi), phi))
+    exact = phi.astype(np.float64) - k.astype(np.float64) * 2 * np.pi
+    assert np.abs(r.astype(np.float64) - exact).max() < 2.5e-7
+    assert np.abs(r).max() <= np.pi + 1e-3
