@@ -91,7 +91,14 @@ __device__ __forceinline__ int sidx(int i, int line) {
 // Barrier over the threads that share an exchange buffer.  SY = 0: the warp
 // (lines of <= 32 threads); SY = 1: the whole CTA; SY = 2: the calling
 // thread's group of 256 threads (named barrier 1 + threadIdx.x / 256), for
-// kernels whose CTA holds several independent tile groups.
+// kernels whose CTA holds several independent tile groups; SY >= 32 (a
+// multiple of 32): the calling thread's group of SY threads (named barrier
+// 1 + threadIdx.x / SY; at most 15 groups per CTA).
+template <int SY>
+constexpr int group_threads() {
+  return SY == 2 ? 256 : SY;
+}
+
 template <int SY>
 __device__ __forceinline__ void group_sync() {
   if constexpr (SY == 0) {
@@ -99,14 +106,16 @@ __device__ __forceinline__ void group_sync() {
   } else if constexpr (SY == 1) {
     __syncthreads();
   } else {
-    asm volatile("bar.sync %0, 256;" ::"r"(1 + (int)(threadIdx.x >> 8)) : "memory");
+    constexpr int GT = group_threads<SY>();
+    static_assert(GT % 32 == 0, "group barriers cover whole warps");
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + (int)(threadIdx.x / GT)), "n"(GT) : "memory");
   }
 }
 
 // Thread index within the exchange group.
 template <int SY>
 __device__ __forceinline__ int group_tid() {
-  if constexpr (SY == 2) return (int)(threadIdx.x & 255u);
+  if constexpr (SY >= 2) return (int)(threadIdx.x % (unsigned)group_threads<SY>());
   else return (int)threadIdx.x;
 }
 
@@ -187,6 +196,10 @@ __device__ __forceinline__ void fft_rest(float2 (&v)[16], float2* buf, const flo
   if constexpr (FftGeo<N>::NST >= 2) fft_stage<N, S, 1, IL, LINES, SY>(v, buf, tw, t, line);
   if constexpr (FftGeo<N>::NST == 3) fft_stage<N, S, 2, IL, LINES, SY>(v, buf, tw, t, line);
 }
+
+struct NoHook {
+  __device__ __forceinline__ void operator()() const {}
+};
 
 __device__ __forceinline__ void conj16(float2 (&v)[16]) {
   static_for<16>([&](auto jc) { v[decltype(jc)::value] = cconj(v[decltype(jc)::value]); });
@@ -391,17 +404,17 @@ __device__ __forceinline__ void row_tile(float2 (&v)[16], float2* out, int tile,
 }
 
 // --------------------------------------------------------------- columns --
-// Spectral multiplier without the mask at (|sy|, sx): H(z) [* d/dz factor].
+// Spectral multiplier without the mask at (qx = sx^2, qy = sy^2): H(z)
+// [* d/dz factor].  (a_hi, a_lo) = 1 - beta*qx, the column constant of the
+// float-float phase (unused by the plain-FP32 variant).
 template <int N>
-__device__ __forceinline__ float2 transfer_value(int sy_abs, int sx, const ColOps& ops) {
-  const float qx = (float)(sx * sx), qy = (float)(sy_abs * sy_abs);
+__device__ __forceinline__ float2 transfer_value_cc(float qx, float a_hi, float a_lo, float qy,
+                                                    const ColOps& ops) {
   bool evan;
   float sv, f;
   if (ops.phase_fp32) {
     f = kz_phase_f32(ops.kp, qx, qy, evan, sv);
   } else {
-    float a_hi, a_lo;
-    column_constant(ops.kp, qx, a_hi, a_lo);
     f = kz_phase_ff(ops.kp, a_hi, a_lo, qy, evan, sv);
   }
   // H = exp(-2*pi*i*f); the adjoint uses conj(H).
@@ -415,23 +428,37 @@ __device__ __forceinline__ float2 transfer_value(int sy_abs, int sx, const ColOp
   return m;
 }
 
+// The same at (|sy|, sx).
+template <int N>
+__device__ __forceinline__ float2 transfer_value(int sy_abs, int sx, const ColOps& ops) {
+  const float qx = (float)(sx * sx), qy = (float)(sy_abs * sy_abs);
+  float a_hi = 0.0f, a_lo = 0.0f;
+  if (!ops.phase_fp32) column_constant(ops.kp, qx, a_hi, a_lo);
+  return transfer_value_cc<N>(qx, a_hi, a_lo, qy, ops);
+}
+
 // Spectral multiply of the thread's 16 points of column kx (rows t + T*j).
 // The transfer function of the tile's C columns is first tabulated in shared
 // memory over |ky| = 0..N/2 (C*(N/2+1) evaluations shared by all threads),
-// then each point reads its entry.  The buffer must be free on entry; it is
-// in use on exit (callers sync before the next transform).
+// then each point reads its entry.  Table entry (a, cc) sits at a*C + cc and
+// thread tid fills column tid % C, so each thread computes its column's
+// float-float constant once.  The buffer must be free on entry; it is in use
+// on exit (callers sync before the next transform).
 template <int N, int C, int SY = 1>
 __device__ __forceinline__ void apply_spectral(float2 (&v)[16], float2* tab, int x0, int c, int t,
                                                const ColOps& ops) {
-  constexpr int T = FftGeo<N>::T, NT = C * T, E = (N / 2 + 1) * C;
+  constexpr int T = FftGeo<N>::T, NT = C * T, HE = N / 2 + 1;
   const int kx = x0 + c;
   if (ops.apply_h) {
+    const int tid = group_tid<SY>();
+    const int cc = tid % C, x = x0 + cc;
+    const int sx = x < N / 2 ? x : x - N;
+    const float qx = (float)(sx * sx);
+    float a_hi = 0.0f, a_lo = 0.0f;
+    if (!ops.phase_fp32) column_constant(ops.kp, qx, a_hi, a_lo);
 #pragma unroll 1
-    for (int i = group_tid<SY>(); i < E; i += NT) {
-      const int cc = i % C, a = i / C;
-      const int x = x0 + cc;
-      tab[i] = transfer_value<N>(a, x < N / 2 ? x : x - N, ops);
-    }
+    for (int a = tid / C; a < HE; a += NT / C)
+      tab[a * C + cc] = transfer_value_cc<N>(qx, a_hi, a_lo, (float)(a * a), ops);
     group_sync<SY>();
   }
   static_for<16>([&](auto jc) {
@@ -467,11 +494,14 @@ __device__ __forceinline__ void load_col(float2 (&v)[16], const float2* in, int 
 // transform; COL_INV spectral multiply then inverse transform; COL_FUSED
 // forward, spectral multiply, inverse (one copy of the transform code:
 // inverse(x) = conj(forward(conj(x)))).  v holds the thread's loaded points;
-// `after_first` runs after the first stage of the first transform.  The
-// buffer (C * BUF float2) must be free on entry.
-template <int N, int MODE, int C, bool CG, int SY = 1, class Hook>
+// `after_first` runs after the first stage of the first transform and
+// `before_store` after the last stage has read the buffer into registers.
+// The buffer (C * BUF float2) must be free on entry; callers sync the group
+// before reusing it.
+template <int N, int MODE, int C, bool CG, int SY = 1, class Hook, class Hook2 = NoHook>
 __device__ __forceinline__ void col_tile(float2 (&v)[16], float2* out, int tile, const ColOps& ops,
-                                         float2* buf, const float2* tw, Hook after_first) {
+                                         float2* buf, const float2* tw, Hook after_first,
+                                         Hook2 before_store = NoHook{}) {
   constexpr int T = FftGeo<N>::T;
   const int tid = group_tid<SY>();
   const int c = tid % C, t = tid / C;
@@ -492,8 +522,8 @@ __device__ __forceinline__ void col_tile(float2 (&v)[16], float2* out, int tile,
       fft_first<N, -1, true, C>(v, buf, t, c);
       if (pass == 0) after_first();
       fft_rest<N, -1, true, C, SY>(v, buf, tw, t, c);
-      group_sync<SY>();
       if (pass == 0) {
+        group_sync<SY>();
         apply_spectral<N, C, SY>(v, buf, x0, c, t, ops);
         group_sync<SY>();
         conj16(v);
@@ -501,14 +531,11 @@ __device__ __forceinline__ void col_tile(float2 (&v)[16], float2* out, int tile,
     }
     conj16(v);
   }
+  before_store();
   float2* dst = out + (size_t)t * N + x;
   static_for<16>([&](auto jc) {
     gst<CG>(dst + (size_t)T * N * decltype(jc)::value, v[decltype(jc)::value]);
   });
 }
-
-struct NoHook {
-  __device__ __forceinline__ void operator()() const {}
-};
 
 }  // namespace lp

@@ -52,6 +52,15 @@
 #ifndef LP_ROW_TMA
 #define LP_ROW_TMA (LP_N >= 4096)
 #endif
+// TMA-staged column kernel (eight-column tiles, 16-byte aligned grids).
+#ifndef LP_COL_TMA
+#define LP_COL_TMA 0
+#endif
+// Preferred shared-memory carveout (percent) of every pass kernel of this
+// size; -1 leaves the driver's default.
+#ifndef LP_CARVEOUT
+#define LP_CARVEOUT -1
+#endif
 // TMA row kernels: equal contiguous tile runs per group on as many SMs as
 // that needs (1), or tiles strided over every SM (0).
 #ifndef LP_TMA_BALANCED
@@ -166,6 +175,96 @@ __global__ void __launch_bounds__(Geo<N>::COL_THREADS, LP_COL_MINB)
 // Set when a bounded wait of this size's kernels gave up (read and cleared by
 // take_async_error on the host).
 __device__ int g_async_err;
+
+#if LP_COL_TMA
+// --------------------------------------------------- TMA-staged columns --
+// Column pass with tiles moved by the tensor-copy (TMA) engine instead of
+// per-thread loads: an eight-column tile (C x N complex64, 64-byte row
+// segments) arrives as 2-D boxes of C x 256 elements in two halves.  The
+// first half of the next tile lands in its own buffer while the current
+// tile is transformed; the second half lands in the exchange buffer as soon
+// as the current tile's last stage has read it, while the threads store
+// their results.  Threads read their 16 points from the landed rows (whole
+// 256-byte warp rows, no bank conflicts); stores stay per-thread.
+template <int N>
+struct ColTma {
+  static constexpr int C = Geo<N>::COLS, H = N / 2, BOX = 256;
+  static constexpr uint32_t HALF_BYTES = (uint32_t)C * H * sizeof(float2);
+  static constexpr size_t XB = (size_t)C * FftGeo<N>::BUF;  // exchange (float2)
+  static constexpr size_t OFF_LAND = XB;
+  static constexpr size_t OFF_TW = OFF_LAND + (size_t)C * H;
+  static constexpr size_t OFF_BAR =
+      ((OFF_TW + FftGeo<N>::TW_SIZE) * sizeof(float2) + 15) / 16 * 16;
+  static constexpr size_t SMEM = OFF_BAR + 2 * sizeof(uint64_t);
+  static_assert((OFF_LAND * sizeof(float2)) % 128 == 0, "TMA destinations are 128-byte aligned");
+};
+
+template <int N, int MODE>
+__global__ void __launch_bounds__(Geo<N>::COL_THREADS, 1)
+    col_kernel_tma(const __grid_constant__ CUtensorMap tin, float2* out, ColOps ops) {
+  using CT = ColTma<N>;
+  constexpr int T = Geo<N>::T, C = CT::C, H = CT::H, BOX = CT::BOX, NU = Geo<N>::COL_UNITS;
+  extern __shared__ __align__(128) float2 smem_ct[];
+  float2* xbuf = smem_ct;
+  float2* land = smem_ct + CT::OFF_LAND;
+  float2* tw = smem_ct + CT::OFF_TW;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<char*>(smem_ct) + CT::OFF_BAR);
+  const int c = threadIdx.x % C, t = threadIdx.x / C;
+  load_twiddles<C * T>(tw);
+  if (threadIdx.x == 0) {
+    mbar_init(bars, 1);
+    mbar_init(bars + 1, 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  const int first = blockIdx.x, step = gridDim.x;
+  const int count = first < NU ? (NU - 1 - first) / step + 1 : 0;
+  // rows half*H .. half*H+H-1 of tile `tile` into dst ([row][C], dense)
+  auto load_half = [&](float2* dst, uint64_t* bar, int tile, int half) {
+    mbar_expect_tx(bar, CT::HALF_BYTES);
+#pragma unroll 1
+    for (int b = 0; b < H / BOX; ++b)
+      tma_load_2d(dst + (size_t)b * BOX * C, &tin, tile * C, half * H + b * BOX, bar);
+  };
+  pdl_wait();
+  pdl_release();
+  if (threadIdx.x == 0 && count > 0) {
+    load_half(land, bars, first, 0);
+    load_half(xbuf, bars + 1, first, 1);
+  }
+  bool ok = true;
+#pragma unroll 1
+  for (int j = 0; j < count; ++j) {
+    const int tile = first + j * step;
+    const bool more = j + 1 < count;
+    ok = mbar_wait(bars, j & 1, &g_async_err) && ok;
+    ok = mbar_wait(bars + 1, j & 1, &g_async_err) && ok;
+    float2 v[16];
+    static_for<8>([&](auto jc) {
+      constexpr int jj = decltype(jc)::value;
+      v[jj] = land[(t + T * jj) * C + c];
+      v[jj + 8] = xbuf[(t + T * jj) * C + c];
+    });
+    __syncthreads();  // both landing areas read
+    if (threadIdx.x == 0 && more) {
+      fence_proxy_async();
+      load_half(land, bars, tile + step, 0);
+    }
+    col_tile<N, MODE, C, false>(v, out, tile, ops, xbuf, tw, NoHook{}, [&] {
+      __syncthreads();  // exchange buffer read by the last stage
+      if (threadIdx.x == 0 && more) {
+        fence_proxy_async();
+        load_half(xbuf, bars + 1, tile + step, 1);
+      }
+    });
+  }
+  if (!ok && threadIdx.x == 0 && count > 0) {
+    // A wait gave up: let both areas' last copies land (bounded) before exit.
+    mbar_wait(bars, (count - 1) & 1, &g_async_err);
+    mbar_wait(bars + 1, (count - 1) & 1, &g_async_err);
+  }
+}
+#endif
 
 // Row pass for N >= 1024 on 16-byte aligned grids.  One CTA per SM holds two
 // independent groups of 256 threads.  A tile is 4096 points (4096/N whole
@@ -307,12 +406,35 @@ cudaError_t init_size() {
       e = cudaFuncSetAttribute(row_kernel_tma<N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                ts);
   }
+#if LP_COL_TMA
+  {
+    const int ts = (int)ColTma<N>::SMEM;
+    for (const void* k : {(const void*)col_kernel_tma<N, COL_FWD>,
+                          (const void*)col_kernel_tma<N, COL_INV>,
+                          (const void*)col_kernel_tma<N, COL_FUSED>})
+      if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, ts);
+  }
+#endif
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(col_kernel<N, COL_FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(col_kernel<N, COL_INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(col_kernel<N, COL_FUSED>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+#if LP_CARVEOUT >= 0
+  for (const void* k : {(const void*)row_kernel<N, -1>, (const void*)row_kernel<N, 1>,
+                        (const void*)col_kernel<N, COL_FWD>, (const void*)col_kernel<N, COL_INV>,
+                        (const void*)col_kernel<N, COL_FUSED>})
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, LP_CARVEOUT);
+#if LP_COL_TMA
+  for (const void* k : {(const void*)col_kernel_tma<N, COL_FWD>,
+                        (const void*)col_kernel_tma<N, COL_INV>,
+                        (const void*)col_kernel_tma<N, COL_FUSED>})
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, LP_CARVEOUT);
+#endif
+#endif
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
   int occ = 0;
   if (e == cudaSuccess)
@@ -350,8 +472,23 @@ cudaError_t launch_row(int inverse, const float2* in, float2* out, const RowOps&
 cudaError_t launch_col(int mode, const float2* in, float2* out, const ColOps& ops,
                        cudaStream_t st) {
   constexpr int N = LP_N;
-  const int grid = grid_for(Geo<N>::COL_UNITS, g_occ_col, g_ctas_col);
   const int bs = Geo<N>::COL_THREADS;
+#if LP_COL_TMA
+  {
+    CUtensorMap tm;
+    if ((reinterpret_cast<uintptr_t>(in) & 15u) == 0 &&
+        grid_tensor_map(&tm, in, N, ColTma<N>::C, ColTma<N>::BOX)) {
+      const int grid = cmin(g_sms, Geo<N>::COL_UNITS);
+      const size_t ts = ColTma<N>::SMEM;
+      switch (mode) {
+        case COL_FWD: return launch_pdl(col_kernel_tma<N, COL_FWD>, grid, bs, ts, st, tm, out, ops);
+        case COL_INV: return launch_pdl(col_kernel_tma<N, COL_INV>, grid, bs, ts, st, tm, out, ops);
+        default: return launch_pdl(col_kernel_tma<N, COL_FUSED>, grid, bs, ts, st, tm, out, ops);
+      }
+    }
+  }
+#endif
+  const int grid = grid_for(Geo<N>::COL_UNITS, g_occ_col, g_ctas_col);
   const size_t sm = Geo<N>::COL_SMEM;
   switch (mode) {
     case COL_FWD: return launch_pdl(col_kernel<N, COL_FWD>, grid, bs, sm, st, in, out, ops);

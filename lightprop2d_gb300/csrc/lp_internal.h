@@ -1,6 +1,7 @@
 // Host-side interfaces shared by the translation units of the backend.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -74,6 +75,12 @@ ColOps make_colops(int n, double area, double wl, double z, bool apply_h, uint32
 void set_lens(RowOps& o, int n, double area, double wl, double f);
 
 const SizeOps* size_ops(int n);
+
+// Tensor map of an n x n complex64 grid at `base` for 2-D TMA boxes of
+// bx x by elements (cached per argument set).  false if the driver entry
+// point is unavailable or the encoding is refused (callers then use their
+// plain-load kernels).
+bool grid_tensor_map(CUtensorMap* out, const void* base, int n, int bx, int by);
 
 // Sets the thread-local text returned by lp_last_error() and returns `s`.
 int set_last_error(int s, const char* msg);
