@@ -323,7 +323,8 @@ lp_status lp_plain_propagate_field(const lp_cfloat* field_in,
  * nothing.  N above 1024 returns LP_ERR_UNSUPPORTED_SIZE.  All calls on a
  * device share that array: calls that overlap on the GPU race (serialise
  * them).  The first call on a device does its one-time set-up; make it
- * before any stream capture. */
+ * before any stream capture (a first call on a capturing stream returns
+ * LP_ERR_NOT_INITIALIZED). */
 lp_status lp_plain_propagate_field_noalloc(const lp_cfloat* field_in,
                                            lp_cfloat* field_out, int n,
                                            double area_size, double wl,

@@ -21,7 +21,8 @@
 //     threads) race on the array: serialise them.
 //   * the first call on a device does the one-time set-up (twiddle tables via
 //     lp_init, and the device address of the array via cudaGetSymbolAddress);
-//     make that first call before any stream capture.
+//     make that first call before any stream capture (a first call made
+//     while its stream is capturing returns LP_ERR_NOT_INITIALIZED).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -51,12 +52,21 @@ lp_status noalloc_fail(lp_status s, const char* msg) {
 // Once per device, with that device current: library set-up and the device
 // address of the static H grid (host code must not pass &g_noalloc_h itself:
 // on the host that name is only a stand-in, not a device address).
-lp_status setup_device(int dev, float2** h_out) {
+// A first call inside stream capture is refused (the set-up copies tables and
+// sets kernel attributes, which would invalidate the caller's capture).
+lp_status setup_device(int dev, cudaStream_t st, float2** h_out) {
   std::lock_guard<std::mutex> lk(g_setup_mu);
   if (g_h_addr[dev]) {
     *h_out = g_h_addr[dev];
     return LP_OK;
   }
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess)
+    return noalloc_fail(LP_ERR_CUDA, "cudaStreamIsCapturing failed");
+  if (cs != cudaStreamCaptureStatusNone)
+    return noalloc_fail(LP_ERR_NOT_INITIALIZED,
+                        "lp_plain_propagate_field_noalloc: first call on this device inside "
+                        "stream capture; make one call (or lp_init) before capturing");
   lp_status s = lp_init(dev);
   if (s != LP_OK) return s;
   void* p = nullptr;
@@ -121,26 +131,18 @@ extern "C" lp_status lp_plain_propagate_field_noalloc(const lp_cfloat* field_in,
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return noalloc_fail(LP_ERR_CUDA, "cudaGetDevice failed");
+  cudaStream_t st = (cudaStream_t)stream;
   float2* h = nullptr;
-  lp_status s = setup_device(dev, &h);
+  lp_status s = setup_device(dev, st, &h);
   if (s != LP_OK) return s;
 
-  cudaStream_t st = (cudaStream_t)stream;
   const SizeOps* so = size_ops(n);
   float2* out = reinterpret_cast<float2*>(field_out);
   const size_t n2 = (size_t)n * n;
   const int grid = (int)((n2 + 255) / 256 < 2432 ? (n2 + 255) / 256 : 2432);
 
-  // Transfer-function constants (same as the fused path).
-  const double dL = area_size / n, val = 1.0 / (n * dL), k0 = 1.0 / wl;
-  KParams kp;
-  const FF beta = ff_from_double((val * wl) * (val * wl));
-  const FF R = ff_from_double(z * k0);
-  kp.beta_hi = beta.hi;
-  kp.beta_lo = beta.lo;
-  kp.R_hi = R.hi;
-  kp.R_lo = R.lo;
-  kp.two_pi_k0 = (float)(2.0 * kPi * k0);
+  // Transfer-function constants (the same function the fused path uses).
+  const KParams kp = make_kparams(n, area_size, wl, z);
 
   ColOps inv = col_ops_none();
   inv.scale = 1.0f / ((float)n * (float)n);

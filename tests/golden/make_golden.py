@@ -1,8 +1,8 @@
 """Generate golden vectors by running the reference lightprop2d 1.0.4 itself.
 
-Run here (where the reference source is mounted) with::
+Run where the reference source is available, giving its checkout path::
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the lightprop2d 1.0.4 checkout>
 
 It imports the reference unchanged.  The one shim it needs is a stand-in for
 ``cp.ndarray``: beam2d.py:135 annotates ``cp.ndarray`` even when cupy is absent,
@@ -242,9 +242,25 @@ def main(ref_path):
     out["modes_constructed"] = Q.field.copy()
     out["modes_constructed_spectrum"] = Q.spectrum.copy()
 
+    # --- config 2 at its full size: Gaussian 2048^2, area 2 mm, 632 nm,
+    #     waist 100 um, complex128, propagate(1 cm) then propagate(9 cm)
+    #     (z = 10 cm).  Kept small: the central 64^2 window, every 16th point
+    #     of the centre row and column, and the total energy.
+    W = lp.Beam2D(2 * lp.mm, 2048, 632 * lp.nm, init_field_gen=lp.gaussian_beam,
+                  init_gen_args=(1, 100 * lp.um))
+    for tag, dz in (("z1", 1.0), ("z10", 9.0)):
+        W.propagate(dz)
+        f = W.field
+        out[f"cfg2_{tag}_window"] = f[992:1056, 992:1056].copy()
+        out[f"cfg2_{tag}_row"] = f[1024, ::16].copy()
+        out[f"cfg2_{tag}_col"] = f[::16, 1024].copy()
+        out[f"cfg2_{tag}_energy"] = np.array(np.sum(np.abs(f) ** 2))
+
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     print("wrote", len(out), "arrays")
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the lightprop2d checkout>")
+    main(sys.argv[1])

@@ -12,7 +12,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def test_reference_arm_json_line():
     env = dict(os.environ)
     env["LP_BENCH_CPU_PROCS"] = "2"
-    p = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1",
+    p = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "2",
                         "--warmup", "3"], cwd=ROOT, env=env, capture_output=True, text=True,
                        timeout=600)
     assert p.returncode == 0, p.stderr[-2000:]
@@ -23,6 +23,10 @@ def test_reference_arm_json_line():
               "cpu_baseline", "e2e"):
         assert k in line, k
     assert line["warmup"] >= 3 and line["value"] > 0 and line["higher_is_better"] is True
+    assert line["steps"] == 2  # the requested steps are run
+    sys.path.insert(0, ROOT)
+    import bench
+    assert line["config"] == bench.bench_config()  # the same config as the GPU arm
     cb = line["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] == 2 and cb["value"] == line["value"]
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"],

@@ -158,3 +158,19 @@ def test_unsupported_npoints(lp):
 def test_missing_init_raises(lp):
     with pytest.raises(ValueError):
         lp.Beam2D(1 * mm, 64, 632 * nm)
+
+
+def test_config2_2048_against_the_reference_run(lp, golden):
+    """Config 2 (Gaussian 2048^2, area 2 mm, 632 nm, waist 100 um) through
+    Beam2D in complex64 against the reference's own complex128 run at
+    z = 1 cm and 10 cm: central window, centre row and column, energy."""
+    b = lp.Beam2D(2 * mm, 2048, 632 * nm, init_field_gen=lp.gaussian_beam,
+                  init_gen_args=(1, 100 * um), complex_bits=64)
+    for tag, dz in (("z1", 1.0), ("z10", 9.0)):
+        b.propagate(dz)
+        f = H(b.field)
+        parts = {"window": f[992:1056, 992:1056], "row": f[1024, ::16], "col": f[::16, 1024]}
+        for k, v in parts.items():
+            assert O.rel_l2(v, golden[f"cfg2_{tag}_{k}"]) < TOL, (tag, k)
+        e = float(np.sum(np.abs(f.astype(np.complex128)) ** 2))
+        assert abs(e - float(golden[f"cfg2_{tag}_energy"])) < TOL * e

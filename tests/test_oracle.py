@@ -166,3 +166,20 @@ def test_modes_oracle_matches_reference(golden):
     c = golden["modes_scalar"] * np.exp(0.5j)
     assert np.allclose(O.modes_combine(m, c, 64), golden["modes_constructed"], rtol=1e-12,
                        atol=1e-15)
+
+
+def _cfg2_parts(f, tag):
+    return {"window": f[992:1056, 992:1056], "row": f[1024, ::16], "col": f[::16, 1024]}
+
+
+def test_config2_2048_reference_run(golden):
+    """Config 2 at its full size (2048^2): the oracle against the reference's
+    own complex128 run at z = 1 cm and 10 cm (window, centre row/column,
+    energy)."""
+    b = O.OracleBeam(2 * mm, 2048, 632 * nm, init_field=O.gaussian(2048, 2 * mm, 1, 100 * um))
+    for tag, dz in (("z1", 1.0), ("z10", 9.0)):
+        b.propagate(dz)
+        for k, v in _cfg2_parts(b.field, tag).items():
+            assert O.rel_l2(v, golden[f"cfg2_{tag}_{k}"]) < 1e-10, (tag, k)
+        e = np.sum(np.abs(b.field) ** 2)
+        assert abs(e - golden[f"cfg2_{tag}_energy"]) < 1e-10 * e
