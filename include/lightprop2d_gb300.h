@@ -20,7 +20,7 @@
  *     per-(device, stream) H grid that lp_workspace_release() frees.
  *   - Errors: every call returns an lp_status; no exception crosses the ABI.
  *     lp_last_error() returns a thread-local message for the last failure.
- *   - Supported N: powers of two from 16 to 4096.  Other N return
+ *   - Supported N: powers of two from 16 to 8192.  Other N return
  *     LP_ERR_UNSUPPORTED_SIZE (the reference accepts any N through numpy).
  *   - Pointers must be 8-byte aligned (complex64); N >= 16 keeps every row
  *     16-byte aligned when the base pointer is.
@@ -45,7 +45,7 @@ typedef struct lp_cfloat {
 typedef enum lp_status {
   LP_OK = 0,
   LP_ERR_INVALID_ARGUMENT = 1,  /* null pointer, bad dtype code, non-finite scalar */
-  LP_ERR_UNSUPPORTED_SIZE = 2,  /* N not a power of two in [16, 4096] */
+  LP_ERR_UNSUPPORTED_SIZE = 2,  /* N not a power of two in [16, 8192] */
   LP_ERR_MISALIGNED = 3,        /* pointer not 8-byte aligned */
   LP_ERR_CUDA = 4,              /* a CUDA runtime call failed (see lp_last_error) */
   LP_ERR_OUT_OF_MEMORY = 5,     /* scratch allocation failed */

@@ -33,7 +33,7 @@ Differences, by design:
   issues one warning.
 * ``use_gpu`` is accepted for signature compatibility; the backend always
   runs on a CUDA device.  ``numpy_output`` works as in the reference.
-* Supported ``npoints``: powers of two from 16 to 4096 (ValueError otherwise).
+* Supported ``npoints``: powers of two from 16 to 8192 (ValueError otherwise).
 """
 from __future__ import annotations
 
@@ -105,7 +105,7 @@ class Beam2D:
         if not B.is_supported(self.npoints):
             raise ValueError(
                 f"npoints={self.npoints} is not supported by the GB300 backend "
-                "(powers of two from 16 to 4096)")
+                "(powers of two from 16 to 8192)")
         if self.complex_bits == 128 and not _warned_c128:
             _warned_c128 = True
             warnings.warn("complex_bits=128: the GB300 backend stores complex64 fields "
@@ -379,7 +379,7 @@ class Beam2D:
     def _check_new_n(self, n, what):
         if not B.is_supported(n):
             raise ValueError(f"{what}: npoints={n} is not supported by the GB300 backend "
-                             "(powers of two from 16 to 4096)")
+                             "(powers of two from 16 to 8192)")
 
     def expand(self, area_size: float):
         """Grow the area to ``area_size`` at constant dL, padding every side

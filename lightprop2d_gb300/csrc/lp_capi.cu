@@ -16,7 +16,7 @@
 
 namespace lp {
 extern const SizeOps size_ops_16, size_ops_32, size_ops_64, size_ops_128, size_ops_256,
-    size_ops_512, size_ops_1024, size_ops_2048, size_ops_4096;
+    size_ops_512, size_ops_1024, size_ops_2048, size_ops_4096, size_ops_8192;
 
 const SizeOps* size_ops(int n) {
   switch (n) {
@@ -29,6 +29,7 @@ const SizeOps* size_ops(int n) {
     case 1024: return &size_ops_1024;
     case 2048: return &size_ops_2048;
     case 4096: return &size_ops_4096;
+    case 8192: return &size_ops_8192;
     default: return nullptr;
   }
 }
@@ -78,7 +79,7 @@ lp_status init_device(int dev) {
   int prev = -1;
   LP_CUDA(cudaGetDevice(&prev), "cudaGetDevice");
   if (prev != dev) LP_CUDA(cudaSetDevice(dev), "cudaSetDevice");
-  static const int sizes[] = {16, 32, 64, 128, 256, 512, 1024, 2048, 4096};
+  static const int sizes[] = {16, 32, 64, 128, 256, 512, 1024, 2048, 4096, 8192};
   for (int n : sizes) {
     cudaError_t e = size_ops(n)->init();
     if (e != cudaSuccess) {
@@ -157,7 +158,7 @@ bool aligned8(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 7u) == 0
 lp_status check_grid(int n) {
   if (!size_ops(n))
     return fail(LP_ERR_UNSUPPORTED_SIZE,
-                "npoints=%d is not supported (powers of two from 16 to 4096)", n);
+                "npoints=%d is not supported (powers of two from 16 to 8192)", n);
   return LP_OK;
 }
 
@@ -253,8 +254,8 @@ __global__ void xmul_kernel(float2* __restrict__ f, int n, RowOps ops) {
     const int y = (int)(i / n), x = (int)(i % n);
     float2 m = make_float2(1.0f, 0.0f);
     if (ops.lens) {
-      const float jx = (float)(x - n / 2), jy = (float)(y - n / 2);
-      m = cis_cycles(lens_cycles(ops.kap_hi, ops.kap_lo, fmaf(jx, jx, jy * jy)), 1.0f);
+      const int jx = x - n / 2, jy = y - n / 2;
+      m = cis_cycles(lens_cycles(ops.kap_hi, ops.kap_lo, jx * jx + jy * jy), 1.0f);
     }
     if (ops.xmask) m = cmul(m, mask_value_xy(ops.xmask, ops.xmask_type, y, x, n));
     if (ops.conj) m = cconj(m);
@@ -407,7 +408,7 @@ lp_status lp_async_status(void* stream) {
   cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "lp_async_status: synchronize");
   int bad = 0;
-  for (int n = 16; n <= 4096; n *= 2) {
+  for (int n = 16; n <= 8192; n *= 2) {
     const int r = size_ops(n)->take_async_error();
     if (r < 0) return fail(LP_ERR_CUDA, "lp_async_status: reading the error record failed");
     bad |= r;

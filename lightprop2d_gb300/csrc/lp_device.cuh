@@ -340,10 +340,15 @@ __device__ __forceinline__ float2 cis_radians(float phi) {
 
 // Lens phase in cycles at integer offsets (jx, jy) from the grid centre:
 // (X^2+Y^2)*k0/(2f) radians = kappa*(jx^2+jy^2) cycles, kappa = dL^2 k0/(4 pi f).
-__device__ __forceinline__ float lens_cycles(float kap_hi, float kap_lo, float m) {
+// m = jx^2 + jy^2 is an exact integer (up to 2^25 at N = 8192); above 2^24 it
+// does not fit a float, so it is split into m_hi = fl(m) and the exact
+// remainder m_lo.
+__device__ __forceinline__ float lens_cycles(float kap_hi, float kap_lo, int m) {
+  const float m_hi = (float)m;
+  const float m_lo = (float)(m - (int)m_hi);
   float c_hi, c_e;
-  two_prod(kap_hi, m, c_hi, c_e);
-  const float c_lo = fmaf(kap_lo, m, c_e);
+  two_prod(kap_hi, m_hi, c_hi, c_e);
+  const float c_lo = fmaf(kap_lo, m_hi, c_e) + kap_hi * m_lo;
   return (c_hi - rintf(c_hi)) + c_lo;
 }
 

@@ -32,44 +32,50 @@ namespace lp {
 
 template <int N>
 struct Plan;  // radices of the stages (0 = no stage)
-template <> struct Plan<16> { static constexpr int R[3] = {16, 0, 0}; };
-template <> struct Plan<32> { static constexpr int R[3] = {16, 2, 0}; };
-template <> struct Plan<64> { static constexpr int R[3] = {16, 4, 0}; };
-template <> struct Plan<128> { static constexpr int R[3] = {16, 8, 0}; };
-template <> struct Plan<256> { static constexpr int R[3] = {16, 16, 0}; };
-template <> struct Plan<512> { static constexpr int R[3] = {16, 16, 2}; };
-template <> struct Plan<1024> { static constexpr int R[3] = {16, 16, 4}; };
-template <> struct Plan<2048> { static constexpr int R[3] = {16, 16, 8}; };
-template <> struct Plan<4096> { static constexpr int R[3] = {16, 16, 16}; };
+template <> struct Plan<16> { static constexpr int R[4] = {16, 0, 0, 0}; };
+template <> struct Plan<32> { static constexpr int R[4] = {16, 2, 0, 0}; };
+template <> struct Plan<64> { static constexpr int R[4] = {16, 4, 0, 0}; };
+template <> struct Plan<128> { static constexpr int R[4] = {16, 8, 0, 0}; };
+template <> struct Plan<256> { static constexpr int R[4] = {16, 16, 0, 0}; };
+template <> struct Plan<512> { static constexpr int R[4] = {16, 16, 2, 0}; };
+template <> struct Plan<1024> { static constexpr int R[4] = {16, 16, 4, 0}; };
+template <> struct Plan<2048> { static constexpr int R[4] = {16, 16, 8, 0}; };
+template <> struct Plan<4096> { static constexpr int R[4] = {16, 16, 16, 0}; };
+template <> struct Plan<8192> { static constexpr int R[4] = {16, 16, 16, 2}; };
 
 constexpr int cmin(int a, int b) { return a < b ? a : b; }
 constexpr int cmax(int a, int b) { return a > b ? a : b; }
 
 template <int N>
 struct FftGeo {
+  using P = Plan<N>;
   static constexpr int T = N / 16;  // threads per line
-  static constexpr int NST = Plan<N>::R[2] ? 3 : Plan<N>::R[1] ? 2 : 1;
+  static constexpr int NST = P::R[3] ? 4 : P::R[2] ? 3 : P::R[1] ? 2 : 1;
   static constexpr int BUF = N + N / 16;  // padded line buffer (float2)
-  // Twiddle table offsets: stage 1 at 0 (R1*16 entries), stage 2 after it.
-  static constexpr int NS1 = 16, NS2 = 16 * Plan<N>::R[1];
-  static constexpr int TW_OFF1 = 0, TW_OFF2 = Plan<N>::R[1] * NS1;
-  static constexpr int TW_SIZE = TW_OFF2 + Plan<N>::R[2] * NS2 + 1;
+  // Twiddles of stage s (s >= 1): W_(NS*R)^(r*k) for r = 1..R-1, k < NS, at
+  // TW_OFF_s + (r-1)*NS + k (the r = 0 row, all ones, is not stored).
+  static constexpr int NS1 = 16, NS2 = 16 * P::R[1], NS3 = NS2 * cmax(P::R[2], 1);
+  static constexpr int TW_OFF1 = 0;
+  static constexpr int TW_OFF2 = TW_OFF1 + cmax(P::R[1] - 1, 0) * NS1;
+  static constexpr int TW_OFF3 = TW_OFF2 + cmax(P::R[2] - 1, 0) * NS2;
+  static constexpr int TW_SIZE = TW_OFF3 + cmax(P::R[3] - 1, 0) * NS3 + 1;
 };
 
-// Host: the stage twiddles of size N, layout per stage [r][k] = W_(Ns*R)^(r*k)
-// (forward sign), computed in double and rounded once.
+// Host: the stage twiddles of size N (forward sign), computed in double and
+// rounded once; layout as in FftGeo.
 template <int N>
 inline void fill_twiddles(float2* tw) {
   using G = FftGeo<N>;
   auto fill = [&](int off, int R, int NS) {
-    for (int r = 0; r < R; ++r)
+    for (int r = 1; r < R; ++r)
       for (int k = 0; k < NS; ++k) {
         const double ang = -2.0 * kPi * (double)(r * k) / (double)(NS * R);
-        tw[off + r * NS + k] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+        tw[off + (r - 1) * NS + k] = make_float2((float)std::cos(ang), (float)std::sin(ang));
       }
   };
   if (G::NST >= 2) fill(G::TW_OFF1, Plan<N>::R[1], G::NS1);
   if (G::NST >= 3) fill(G::TW_OFF2, Plan<N>::R[2], G::NS2);
+  if (G::NST >= 4) fill(G::TW_OFF3, Plan<N>::R[3], G::NS3);
   tw[G::TW_SIZE - 1] = make_float2(1.0f, 0.0f);
 }
 
@@ -150,8 +156,8 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[16], float2* buf, const fl
                                           int line) {
   using G = FftGeo<N>;
   constexpr int R = Plan<N>::R[s], T = G::T, nb = 16 / R;
-  constexpr int NS = (s == 1) ? G::NS1 : G::NS2;
-  constexpr int OFF = (s == 1) ? G::TW_OFF1 : G::TW_OFF2;
+  constexpr int NS = (s == 1) ? G::NS1 : (s == 2) ? G::NS2 : G::NS3;
+  constexpr int OFF = (s == 1) ? G::TW_OFF1 : (s == 2) ? G::TW_OFF2 : G::TW_OFF3;
   constexpr bool LAST = (s == G::NST - 1);
   group_sync<SY>();
   static_for<nb>([&](auto qc) {
@@ -171,7 +177,7 @@ __device__ __forceinline__ void fft_stage(float2 (&v)[16], float2* buf, const fl
     static_for<R>([&](auto rc) { a[decltype(rc)::value] = v[q + nb * decltype(rc)::value]; });
     static_for<R - 1>([&](auto rc) {
       constexpr int r = decltype(rc)::value + 1;
-      float2 w = tw[OFF + r * NS + k];
+      float2 w = tw[OFF + (r - 1) * NS + k];
       if constexpr (S > 0) w.y = -w.y;
       a[r] = cmul(a[r], w);
     });
@@ -194,7 +200,8 @@ template <int N, int S, bool IL, int LINES, int SY>
 __device__ __forceinline__ void fft_rest(float2 (&v)[16], float2* buf, const float2* tw, int t,
                                          int line) {
   if constexpr (FftGeo<N>::NST >= 2) fft_stage<N, S, 1, IL, LINES, SY>(v, buf, tw, t, line);
-  if constexpr (FftGeo<N>::NST == 3) fft_stage<N, S, 2, IL, LINES, SY>(v, buf, tw, t, line);
+  if constexpr (FftGeo<N>::NST >= 3) fft_stage<N, S, 2, IL, LINES, SY>(v, buf, tw, t, line);
+  if constexpr (FftGeo<N>::NST >= 4) fft_stage<N, S, 3, IL, LINES, SY>(v, buf, tw, t, line);
 }
 
 struct NoHook {
@@ -300,11 +307,11 @@ __device__ __forceinline__ void apply_xops(float2 (&v)[16], float2* slots, int n
   constexpr int T = FftGeo<N>::T;
   const int tid = group_tid<SY>();
   if (ops.lens) {
-    const float jy = (float)(y - N / 2);
+    const int jy = y - N / 2;
 #pragma unroll 1
     for (int j = 0; j < 16; ++j) {
-      const float jx = (float)(t + T * j - N / 2);
-      float2 m = cis_cycles(lens_cycles(ops.kap_hi, ops.kap_lo, fmaf(jx, jx, jy * jy)), 1.0f);
+      const int jx = t + T * j - N / 2;
+      float2 m = cis_cycles(lens_cycles(ops.kap_hi, ops.kap_lo, jx * jx + jy * jy), 1.0f);
       if (ops.conj) m = cconj(m);
       slots[j * nthreads + tid] = m;
     }
@@ -341,7 +348,7 @@ __device__ __forceinline__ void tile_moments(const float2 (&v)[16], int y, int t
   });
   const double jy = (double)(y - N / 2);
   double m[5] = {(double)s0, (double)s1, jy * s0, (double)s3, jy * jy * s0};
-  __shared__ double red[2][5][8];  // [group][value][warp of the group]
+  __shared__ double red[2][5][32];  // [group][value][warp of the group]
   const int tid = group_tid<SY>(), lane = tid & 31, w = tid >> 5;
   const int grp = SY == 2 ? (int)(threadIdx.x >> 8) : 0;
 #pragma unroll
@@ -354,7 +361,7 @@ __device__ __forceinline__ void tile_moments(const float2 (&v)[16], int y, int t
   if (tid < 5) {
     double a = 0.0;
     const int nw = (SY == 2 ? 256 : (int)blockDim.x) >> 5;
-    for (int i = 0; i < nw && i < 8; ++i) a += red[grp][tid][i];
+    for (int i = 0; i < nw; ++i) a += red[grp][tid][i];
     atomicAdd(out + tid, a);
   }
   group_sync<SY>();

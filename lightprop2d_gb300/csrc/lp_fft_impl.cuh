@@ -28,12 +28,17 @@
 #ifndef LP_COL_C4096
 #define LP_COL_C4096 4
 #endif
+// 8192: a line is 512 threads and 68 KB of exchange buffer, so column tiles
+// hold two columns (1024 threads, 204 KB with the twiddles).
+#ifndef LP_COL_C8192
+#define LP_COL_C8192 2
+#endif
 // Per-size choices below were measured on GB300 (fused propagate, inputs
 // larger than L2); each can be overridden with -D for tuning experiments.
 // 1: load the next tile into a second register set while transforming the
 // current one; 0: load it at the top of the next iteration.
 #ifndef LP_ROW_PREFETCH
-#define LP_ROW_PREFETCH 1
+#define LP_ROW_PREFETCH (LP_N < 8192)
 #endif
 #ifndef LP_COL_PREFETCH
 #define LP_COL_PREFETCH 0
@@ -50,8 +55,10 @@
 // N >= 1024 only.  TMA wins at 4096 (rows of 32 KB); at 1024-2048 the
 // register kernels, which use every SM, are faster.
 #ifndef LP_ROW_TMA
-#define LP_ROW_TMA (LP_N >= 4096)
+#define LP_ROW_TMA (LP_N == 4096)
 #endif
+// The TMA row kernel's tiles are 4096 points of whole rows: N in 1024..4096.
+#define LP_ROW_TMA_SIZE (LP_N >= 1024 && LP_N <= 4096)
 // TMA-staged column kernel (eight-column tiles, 16-byte aligned grids).
 #ifndef LP_COL_TMA
 #define LP_COL_TMA 0
@@ -76,7 +83,8 @@ struct Geo : FftGeo<N> {
   // rows per CTA: 256 threads for large N, one warp's worth for small N
   static constexpr int ROWS = N >= 1024 ? cmax(1, 256 / F::T) : cmin(N, cmax(1, 32 / F::T));
   // columns per CTA: at least 4 so every row segment is a full 32-byte sector
-  static constexpr int COLS = N >= 4096   ? LP_COL_C4096
+  static constexpr int COLS = N >= 8192   ? LP_COL_C8192
+                              : N >= 4096 ? LP_COL_C4096
                               : N >= 2048 ? LP_COL_C2048
                               : N >= 1024 ? LP_COL_C1024
                                           : cmin(N, cmax(4, 32 / F::T));
@@ -266,6 +274,7 @@ __global__ void __launch_bounds__(Geo<N>::COL_THREADS, 1)
 }
 #endif
 
+#if LP_ROW_TMA_SIZE
 // Row pass for N >= 1024 on 16-byte aligned grids.  One CTA per SM holds two
 // independent groups of 256 threads.  A tile is 4096 points (4096/N whole
 // rows, contiguous in memory); each group owns a contiguous run of `tpg`
@@ -350,6 +359,8 @@ __global__ void __launch_bounds__(512, 1)
   }
 }
 
+#endif
+
 // ------------------------------------------------------------- launchers --
 int g_sms = 0;                       // SM count of the device set up last
 int g_occ_row = 1, g_occ_col = 1;    // max resident CTAs per SM
@@ -397,7 +408,8 @@ cudaError_t init_size() {
     e = cudaFuncSetAttribute(row_kernel<N, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(row_kernel<N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs);
-  if constexpr (N >= 1024) {
+#if LP_ROW_TMA_SIZE
+  {
     const int ts = (int)RowTma<N>::SMEM;
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(row_kernel_tma<N, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -406,6 +418,7 @@ cudaError_t init_size() {
       e = cudaFuncSetAttribute(row_kernel_tma<N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                ts);
   }
+#endif
 #if LP_COL_TMA
   {
     const int ts = (int)ColTma<N>::SMEM;
@@ -451,7 +464,8 @@ cudaError_t init_size() {
 cudaError_t launch_row(int inverse, const float2* in, float2* out, const RowOps& ops,
                        cudaStream_t st) {
   constexpr int N = LP_N;
-  if constexpr (N >= 1024 && LP_ROW_TMA) {
+#if LP_ROW_TMA_SIZE && LP_ROW_TMA
+  {
     if ((reinterpret_cast<uintptr_t>(in) & 15u) == 0) {
       using RT = RowTma<N>;
       const int tpg = (RT::NU + RT::G * g_sms - 1) / (RT::G * g_sms);
@@ -461,6 +475,7 @@ cudaError_t launch_row(int inverse, const float2* in, float2* out, const RowOps&
                         RT::SMEM, st, in, out, ops, tpg);
     }
   }
+#endif
   const int grid = grid_for(Geo<N>::ROW_UNITS, g_occ_row, g_ctas_row);
   if (inverse)
     return launch_pdl(row_kernel<N, 1>, grid, Geo<N>::ROW_THREADS, Geo<N>::ROW_SMEM, st, in, out,

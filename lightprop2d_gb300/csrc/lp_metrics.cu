@@ -139,7 +139,7 @@ extern "C" lp_status lp_beam_moments(const lp_cfloat* field, int n, double* mome
   using namespace lp;
   if (!lp_is_supported_n(n))
     return (lp_status)set_last_error(LP_ERR_UNSUPPORTED_SIZE,
-                                     "lp_beam_moments: npoints must be a power of two in 16..4096");
+                                     "lp_beam_moments: npoints must be a power of two in 16..8192");
   if (!field || !moments)
     return (lp_status)set_last_error(LP_ERR_INVALID_ARGUMENT, "lp_beam_moments: NULL pointer");
   if ((reinterpret_cast<uintptr_t>(field) & 7u) || (reinterpret_cast<uintptr_t>(moments) & 7u))

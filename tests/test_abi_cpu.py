@@ -39,9 +39,9 @@ def test_every_declared_symbol_is_exported(lib):
 
 def test_meta_calls(lib):
     assert lib.lp_abi_version() == 1
-    for n in (16, 32, 64, 128, 256, 512, 1024, 2048, 4096):
+    for n in (16, 32, 64, 128, 256, 512, 1024, 2048, 4096, 8192):
         assert lib.lp_is_supported_n(n) == 1
-    for n in (0, 8, 100, 8192, -4):
+    for n in (0, 8, 100, 16384, -4):
         assert lib.lp_is_supported_n(n) == 0
     assert lib.lp_status_string(0) == b"ok"
 

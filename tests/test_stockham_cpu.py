@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 PLAN = {16: (16,), 32: (16, 2), 64: (16, 4), 128: (16, 8), 256: (16, 16), 512: (16, 16, 2),
-        1024: (16, 16, 4), 2048: (16, 16, 8), 4096: (16, 16, 16)}
+        1024: (16, 16, 4), 2048: (16, 16, 8), 4096: (16, 16, 16), 8192: (16, 16, 16, 2)}
 
 
 def stockham(x, sign=-1, dtype=np.complex128):
