@@ -70,10 +70,14 @@ typedef enum lp_mask_type {
    *                     square_hole, square_slits, plane_wave)
    *   LP_MASK_SPAN_I32: int32 lo[N], hi[N];    multiplier 1 if lo[ix] <= iy < hi[ix]
    *                     else 0 (round_hole); x-domain masks only.
+   *   LP_MASK_SEP_C64:  complex64 fx[N], fy[N]; multiplier fx[ix] * fy[iy]
+   *                     (separable complex multipliers; the chirp kernels of
+   *                     the transforms for sizes that are not powers of two)
    * The host builds the tables with the reference's own float64 arithmetic
    * (lightprop2d_gb300/generators.py), so boolean edges match it exactly. */
   LP_MASK_SEP_F32 = 7,
-  LP_MASK_SPAN_I32 = 8
+  LP_MASK_SPAN_I32 = 8,
+  LP_MASK_SEP_C64 = 9
 } lp_mask_type;
 
 /* Flags (bitwise OR). */

@@ -32,6 +32,7 @@ LP_MASK_F64 = 5
 LP_MASK_C128 = 6
 LP_MASK_SEP_F32 = 7
 LP_MASK_SPAN_I32 = 8
+LP_MASK_SEP_C64 = 9
 
 # flags
 LP_FLAG_PHASE_FP32 = 0x1

@@ -246,7 +246,7 @@ lp_status lp_batch_create(const lp_beam_desc* beams, int count, const lp_batch_o
   const int glog = opt.group_points_log2 > 0 ? opt.group_points_log2 : 23;
   for (int i = 0; i < count; ++i) {
     const lp_beam_desc& b = beams[i];
-    if (b.n < 64 || b.n > 4096 || !lp_is_supported_n(b.n)) {
+    if (b.n < 64 || b.n > 4096 || (b.n & (b.n - 1)) != 0) {
       char msg[128];
       snprintf(msg, sizeof(msg), "beam %d: n=%d unsupported in a batch (64..4096, power of two)",
                i, b.n);

@@ -122,6 +122,8 @@ lp_status ensure_ready(cudaStream_t st, int* dev_out) {
 struct Scratch {
   void* hbuf = nullptr;
   size_t hbuf_bytes = 0;
+  void* blue = nullptr;  // M x M work grid of the transforms for other sizes
+  size_t blue_bytes = 0;
   void* kz = nullptr;
   size_t kz_bytes = 0;
   int kz_n = 0;
@@ -152,13 +154,49 @@ Scratch& scratch_for(int dev, cudaStream_t st) {
   return g_scratch[std::make_pair(dev, (uintptr_t)st)];
 }
 
+#define LP_TRY(x)                  \
+  do {                             \
+    lp_status s_ = (x);            \
+    if (s_ != LP_OK) return s_;    \
+  } while (0)
+
 // ---------------------------------------------------------------- checks --
 bool aligned8(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 7u) == 0; }
 
 lp_status check_grid(int n) {
-  if (!size_ops(n))
+  if (!size_ops(n) && !bluestein_n(n))
     return fail(LP_ERR_UNSUPPORTED_SIZE,
-                "npoints=%d is not supported (powers of two from 16 to 8192)", n);
+                "npoints=%d is not supported (2..4096, or a power of two up to 8192)", n);
+  return LP_OK;
+}
+
+// Work grid of the transforms for sizes other than the power-of-two kernels'
+// (per device and stream; grown with cudaMalloc, which is refused inside a
+// stream capture: make one call of that size first).
+lp_status blue_workspace(int dev, cudaStream_t st, int n, float2** ws) {
+  const int m = bluestein_m(n);
+  const size_t need = sizeof(float2) * (size_t)m * m;
+  std::lock_guard<std::mutex> lk(g_mu);
+  Scratch& s = g_scratch[std::make_pair(dev, (uintptr_t)st)];
+  if (s.blue_bytes < need) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    LP_CUDA(cudaStreamIsCapturing(st, &cs), "cudaStreamIsCapturing");
+    if (cs != cudaStreamCaptureStatusNone)
+      return fail(LP_ERR_NOT_INITIALIZED,
+                  "npoints=%d needs a %dx%d work grid: make one call of this size before "
+                  "stream capture", n, m, m);
+    LP_TRY(grow(&s.blue, &s.blue_bytes, need, "transform work grid"));
+  }
+  *ws = reinterpret_cast<float2*>(s.blue);
+  return LP_OK;
+}
+
+lp_status blue_call(cudaError_t e, const char* what) {
+  if (e == cudaErrorStreamCaptureUnsupported)
+    return fail(LP_ERR_NOT_INITIALIZED,
+                "%s: the first transform of this grid size builds tables; make it before "
+                "stream capture", what);
+  if (e != cudaSuccess) return cuda_fail(e, what);
   return LP_OK;
 }
 
@@ -169,7 +207,7 @@ lp_status check_ptr(const void* p, const char* name, bool required) {
 }
 
 lp_status check_mask(const void* m, int type, const char* name, bool k_domain = false) {
-  if (type < LP_MASK_NONE || type > LP_MASK_SPAN_I32)
+  if (type < LP_MASK_NONE || type > LP_MASK_SEP_C64)
     return fail(LP_ERR_INVALID_ARGUMENT, "%s: unknown mask type %d", name, type);
   if (k_domain && type == LP_MASK_SPAN_I32)
     return fail(LP_ERR_INVALID_ARGUMENT, "%s: LP_MASK_SPAN_I32 is an x-domain mask type", name);
@@ -177,7 +215,8 @@ lp_status check_mask(const void* m, int type, const char* name, bool k_domain = 
   if (!m) return fail(LP_ERR_INVALID_ARGUMENT, "%s: NULL with mask type %d", name, type);
   const uintptr_t a = reinterpret_cast<uintptr_t>(m);
   const uintptr_t need = (type == LP_MASK_U8) ? 1 : (type == LP_MASK_C128) ? 16
-                         : (type == LP_MASK_C64 || type == LP_MASK_F64) ? 8 : 4;
+                         : (type == LP_MASK_C64 || type == LP_MASK_F64 || type == LP_MASK_SEP_C64)
+                             ? 8 : 4;
   if (a % need) return fail(LP_ERR_MISALIGNED, "%s is not %zu-byte aligned", name, (size_t)need);
   return LP_OK;
 }
@@ -189,11 +228,6 @@ lp_status check_geometry(double area, double wl) {
   return LP_OK;
 }
 
-#define LP_TRY(x)                  \
-  do {                             \
-    lp_status s_ = (x);            \
-    if (s_ != LP_OK) return s_;    \
-  } while (0)
 
 }  // namespace
 
@@ -254,7 +288,8 @@ __global__ void xmul_kernel(float2* __restrict__ f, int n, RowOps ops) {
     const int y = (int)(i / n), x = (int)(i % n);
     float2 m = make_float2(1.0f, 0.0f);
     if (ops.lens) {
-      const int jx = x - n / 2, jy = y - n / 2;
+      // X = arange(-n//2, n//2) * dL (beam2d.py:299-300): centre (n+1)/2
+      const int jx = x - (n + 1) / 2, jy = y - (n + 1) / 2;
       m = cis_cycles(lens_cycles(ops.kap_hi, ops.kap_lo, jx * jx + jy * jy), 1.0f);
     }
     if (ops.xmask) m = cmul(m, mask_value_xy(ops.xmask, ops.xmask_type, y, x, n));
@@ -266,7 +301,8 @@ __global__ void xmul_kernel(float2* __restrict__ f, int n, RowOps ops) {
 // Transfer function at point i of an N x N spectrum (float-float phase).
 __device__ __forceinline__ float2 transfer_at(size_t i, int n, const ColOps& ops) {
   const int ky = (int)(i / n), kx = (int)(i % n);
-  const int sx = kx < n / 2 ? kx : kx - n, sy = ky < n / 2 ? ky : ky - n;
+  // fftfreq order (beam2d.py:205): k for k < (n+1)/2, k - n above
+  const int sx = kx < (n + 1) / 2 ? kx : kx - n, sy = ky < (n + 1) / 2 ? ky : ky - n;
   const float qx = (float)(sx * sx), qy = (float)(sy * sy);
   bool evan;
   float sv, f;
@@ -372,7 +408,7 @@ const char* lp_status_string(int s) {
   }
 }
 
-int lp_is_supported_n(int n) { return size_ops(n) ? 1 : 0; }
+int lp_is_supported_n(int n) { return (size_ops(n) || bluestein_n(n)) ? 1 : 0; }
 
 int lp_tune_ctas_per_sm(int n, int kind, int value) {
   const SizeOps* so = size_ops(n);
@@ -396,10 +432,11 @@ lp_status lp_workspace_release(void) {
   for (auto& kv : g_scratch) {
     cudaSetDevice(kv.first.first);
     Scratch& s = kv.second;
-    for (void* p : {s.hbuf, s.kz})
+    for (void* p : {s.hbuf, s.kz, s.blue})
       if (p && cudaFree(p) != cudaSuccess) r = fail(LP_ERR_CUDA, "cudaFree failed");
   }
   g_scratch.clear();
+  bluestein_release();
   cudaSetDevice(prev);
   return r;
 }
@@ -435,6 +472,13 @@ lp_status lp_fft2(const lp_cfloat* in, lp_cfloat* out, int n, int inverse, void*
   const SizeOps* so = size_ops(n);
   const float2* src = reinterpret_cast<const float2*>(in);
   float2* dst = reinterpret_cast<float2*>(out);
+  if (!so) {  // other sizes: Bluestein through a power-of-two work grid
+    float2* ws;
+    LP_TRY(blue_workspace(dev, st, n, &ws));
+    return blue_call(bluestein_dft2(src, dst, n, inverse ? 1 : 0,
+                                    inverse ? 1.0f / ((float)n * (float)n) : 1.0f, ws, st),
+                     "fft2");
+  }
   if (!inverse) return run_fft2_fwd(so, src, dst, row_ops_none(), st);
   ColOps c = col_ops_none();
   c.scale = 1.0f / ((float)n * (float)n);
@@ -464,6 +508,13 @@ lp_status lp_propagate(lp_cfloat* spectrum, lp_cfloat* field, int n, double area
   c.kmask_type = kmask_type;
   if (!(flags & LP_FLAG_SPECTRUM_READONLY)) c.spectrum_out = reinterpret_cast<float2*>(spectrum);
   c.scale = 1.0f / ((float)n * (float)n);
+  if (!so) {  // other sizes: pointwise multipliers, then a Bluestein inverse transform
+    float2* ws;
+    LP_TRY(blue_workspace(dev, st, n, &ws));
+    LP_CUDA(generic_spectral(reinterpret_cast<const float2*>(spectrum), f, n, c, st),
+            "spectral multipliers");
+    return blue_call(bluestein_dft2(f, f, n, 1, 1.0f, ws, st), "inverse transform");
+  }
   mark(0, st);
   LP_CUDA(so->col(COL_INV, reinterpret_cast<const float2*>(spectrum), f, c, st),
           "column pass (transfer + inverse)");
@@ -521,6 +572,28 @@ lp_status lp_propagate_field(const lp_cfloat* field_in, lp_cfloat* field_out,
   c.spectrum_out = reinterpret_cast<float2*>(spectrum_out);
   c.scale = 1.0f / ((float)n * (float)n);
 
+  if (!so) {
+    // Other sizes: the same operator as the fused passes, composed of
+    // pointwise passes and Bluestein transforms.
+    float2* ws;
+    LP_TRY(blue_workspace(dev, st, n, &ws));
+    const float2* src = reinterpret_cast<const float2*>(field_in);
+    if (r.lens || r.xmask) {
+      LP_CUDA(generic_xmul(src, out, n, r, st), "x-domain multipliers");
+      src = out;
+    }
+    LP_TRY(blue_call(bluestein_dft2(src, out, n, 0, 1.0f, ws, st), "forward transform"));
+    LP_CUDA(generic_spectral(out, out, n, c, st), "spectral multipliers");
+    LP_TRY(blue_call(bluestein_dft2(out, out, n, 1, 1.0f, ws, st), "inverse transform"));
+    if (e.lens || e.xmask) LP_CUDA(generic_xmul(out, out, n, e, st), "x-domain multipliers");
+    if (iprofile_out) {
+      const size_t n2 = (size_t)n * n;
+      iprofile_kernel<<<ew_grid(n2), 256, 0, st>>>(out, iprofile_out, n2);
+      LP_CUDA(cudaGetLastError(), "iprofile");
+    }
+    return LP_OK;
+  }
+
   mark(0, st);
   LP_CUDA(so->row(0, reinterpret_cast<const float2*>(field_in), out, r, st),
           "row pass (forward)");
@@ -542,6 +615,13 @@ static lp_status xdomain_op(lp_cfloat* field, lp_cfloat* spectrum_out, int n, Ro
   xmul_kernel<<<ew_grid(n2), 256, 0, st>>>(f, n, r);
   LP_CUDA(cudaGetLastError(), "x-domain multiply");
   if (!spectrum_out) return LP_OK;
+  if (!size_ops(n)) {
+    float2* ws;
+    LP_TRY(blue_workspace(dev, st, n, &ws));
+    return blue_call(bluestein_dft2(f, reinterpret_cast<float2*>(spectrum_out), n, 0, 1.0f, ws,
+                                    st),
+                     "fft2");
+  }
   return run_fft2_fwd(size_ops(n), f, reinterpret_cast<float2*>(spectrum_out), row_ops_none(),
                       st);
 }
@@ -613,7 +693,9 @@ lp_status lp_apply_transfer(lp_cfloat* spectrum, int n, double area_size, double
 lp_status lp_plain_propagate_field(const lp_cfloat* field_in, lp_cfloat* field_out, int n,
                                    double area_size, double wl, double z, uint32_t flags,
                                    void* stream) {
-  LP_TRY(check_grid(n));
+  if (!size_ops(n))
+    return fail(LP_ERR_UNSUPPORTED_SIZE,
+                "lp_plain_propagate_field: npoints=%d (powers of two from 16 to 8192)", n);
   LP_TRY(check_ptr(field_in, "field_in", true));
   LP_TRY(check_ptr(field_out, "field_out", true));
   LP_TRY(check_geometry(area_size, wl));

@@ -374,8 +374,13 @@ __device__ __forceinline__ float2 mask_value(const void* mask, int type, size_t 
 }
 
 // Multiplier at row y, column x of an N x N mask of any type, including the
-// compact generator tables (7: separable fx[x]*fy[y], 8: per-column row span).
+// compact generator tables (7: separable fx[x]*fy[y], 8: per-column row span,
+// 9: complex separable fx[x]*fy[y]).
 __device__ __forceinline__ float2 mask_value_xy(const void* mask, int type, int y, int x, int n) {
+  if (type == 9) {
+    const float2* t = reinterpret_cast<const float2*>(mask);
+    return cmul(__ldg(t + x), __ldg(t + n + y));
+  }
   if (type == 7) {
     const float* t = reinterpret_cast<const float*>(mask);
     return make_float2(__ldg(t + x) * __ldg(t + n + y), 0.0f);

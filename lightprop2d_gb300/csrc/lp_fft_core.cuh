@@ -283,6 +283,17 @@ __device__ __forceinline__ void apply_mask_row(float2 (&v)[16], const void* mask
       });
       break;
     }
+    case 9: {  // complex separable table: fx[x] * fy[y]
+      const float2* fx = reinterpret_cast<const float2*>(mask);
+      float2 fy = __ldg(fx + N + y);
+      if (conj) fy = cconj(fy);
+      float2 m[16];
+      static_for<16>([&](auto jc) { m[jc.value] = __ldg(fx + t + T * jc.value); });
+      static_for<16>([&](auto jc) {
+        v[jc.value] = cmul(cmul(v[jc.value], conj ? cconj(m[jc.value]) : m[jc.value]), fy);
+      });
+      break;
+    }
     default: {  // float64, complex128: rolled
 #pragma unroll 1
       for (int j = 0; j < 16; ++j) {

@@ -76,6 +76,26 @@ void set_lens(RowOps& o, int n, double area, double wl, double f);
 
 const SizeOps* size_ops(int n);
 
+// Grid sizes outside the power-of-two pass kernels (lp_bluestein.cu): n in
+// 2..4096 that is not a power of two in 16..8192.
+bool bluestein_n(int n);
+// The power-of-two size M >= 2n-1 of the Bluestein convolution grid.
+int bluestein_m(int n);
+// n x n 2-D DFT (forward, or unscaled inverse) times `scale`, through an
+// M x M work grid `ws` (M = bluestein_m(n)); in may equal out.  The first
+// call for a size on a device builds its tables (cudaMalloc + copy) and is
+// refused inside stream capture (cudaErrorStreamCaptureUnsupported).
+cudaError_t bluestein_dft2(const float2* in, float2* out, int n, int inverse, float scale,
+                           float2* ws, cudaStream_t st);
+// Pointwise x-domain multipliers (RowOps: lens, mask, conj) and spectral
+// multipliers (ColOps: H, d/dz, kmask, spectrum write, scale) for any n.
+cudaError_t generic_xmul(const float2* in, float2* out, int n, const RowOps& ops,
+                         cudaStream_t st);
+cudaError_t generic_spectral(const float2* in, float2* out, int n, const ColOps& ops,
+                             cudaStream_t st);
+// Frees the Bluestein tables of every device.
+void bluestein_release();
+
 // Tensor map of an n x n complex64 grid at `base` for 2-D TMA boxes of
 // bx x by elements (cached per argument set).  false if the driver entry
 // point is unavailable or the encoding is refused (callers then use their

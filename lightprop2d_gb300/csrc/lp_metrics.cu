@@ -5,7 +5,7 @@
 //   pass 2:  m3 = sum (jx - xc)^2 I,  m4 = sum (jy - yc)^2 I,
 //            xc = m1/m0, yc = m2/m0 read from pass 1's result on the device
 //
-// with I = |field|^2 and jx = ix - n/2, jy = iy - n/2 (grid-index offsets
+// with I = |field|^2 and jx = ix - n/2, jy = iy - n/2 (n even; grid-index offsets
 // from the centre; the caller scales by dL).  The second moments are taken
 // about the centroid, as the reference does, so an off-centre beam loses no
 // precision to cancellation.  Each thread accumulates in FP32 over a strided
@@ -73,16 +73,16 @@ __device__ __forceinline__ void cta_add(const float (&v)[K], double* out) {
 // of n, so a thread's points all lie in one column: its jx is a constant
 // (sum jx I = jx * sum I) and jy advances by stride / n rows per step.
 __global__ void __launch_bounds__(kThreads) moments1_kernel(const float2* __restrict__ f,
-                                                            int logn, double* out) {
+                                                            int n, double* out) {
   // let the second pass's CTAs be scheduled as this pass's CTAs retire
   asm volatile("griddepcontrol.launch_dependents;");
-  const int n = 1 << logn, h = n >> 1;
+  const int h = n >> 1;
   const int n2 = n * n;
   const int stride = (int)gridDim.x * kThreads;
   const int first = (int)blockIdx.x * kThreads + (int)threadIdx.x;
-  const float jx = (float)((first & (n - 1)) - h);
-  const float djy = (float)(stride >> logn);
-  float jy = (float)((first >> logn) - h);
+  const float jx = (float)((first % n) - h);
+  const float djy = (float)(stride / n);
+  float jy = (float)((first / n) - h);
   float s0 = 0.0f, s2 = 0.0f;
   for (int i0 = first; i0 < n2; i0 += kUnroll * stride) {
     float2 v[kUnroll];
@@ -100,8 +100,8 @@ __global__ void __launch_bounds__(kThreads) moments1_kernel(const float2* __rest
 }
 
 __global__ void __launch_bounds__(kThreads) moments2_kernel(const float2* __restrict__ f,
-                                                            int logn, double* out) {
-  const int n = 1 << logn, h = n >> 1;
+                                                            int n, double* out) {
+  const int h = n >> 1;
   const int n2 = n * n;
   const int stride = (int)gridDim.x * kThreads;
   const int first = (int)blockIdx.x * kThreads + (int)threadIdx.x;
@@ -110,9 +110,9 @@ __global__ void __launch_bounds__(kThreads) moments2_kernel(const float2* __rest
   const double m0 = out[0];
   const float xc = m0 > 0.0 ? (float)(out[1] / m0) : 0.0f;
   const float yc = m0 > 0.0 ? (float)(out[2] / m0) : 0.0f;
-  const float dx = (float)((first & (n - 1)) - h) - xc;
-  const float ddy = (float)(stride >> logn);
-  float dy = (float)((first >> logn) - h) - yc;
+  const float dx = (float)((first % n) - h) - xc;
+  const float ddy = (float)(stride / n);
+  float dy = (float)((first / n) - h) - yc;
   float s0 = 0.0f, s1 = 0.0f;
   for (int i0 = first; i0 < n2; i0 += kUnroll * stride) {
     float2 v[kUnroll];
@@ -137,9 +137,11 @@ int g_sms_metrics = 0;
 extern "C" lp_status lp_beam_moments(const lp_cfloat* field, int n, double* moments,
                                      void* stream) {
   using namespace lp;
-  if (!lp_is_supported_n(n))
-    return (lp_status)set_last_error(LP_ERR_UNSUPPORTED_SIZE,
-                                     "lp_beam_moments: npoints must be a power of two in 16..8192");
+  if (!lp_is_supported_n(n) || (n & 1))
+    return (lp_status)set_last_error(
+        LP_ERR_UNSUPPORTED_SIZE,
+        "lp_beam_moments: npoints must be even and supported (the reference's index grid "
+        "mgrid[-n//2:n//2] does not match an odd npoints)");
   if (!field || !moments)
     return (lp_status)set_last_error(LP_ERR_INVALID_ARGUMENT, "lp_beam_moments: NULL pointer");
   if ((reinterpret_cast<uintptr_t>(field) & 7u) || (reinterpret_cast<uintptr_t>(moments) & 7u))
@@ -150,21 +152,25 @@ extern "C" lp_status lp_beam_moments(const lp_cfloat* field, int n, double* mome
     cudaDeviceGetAttribute(&g_sms_metrics, cudaDevAttrMultiProcessorCount, dev);
     if (g_sms_metrics <= 0) g_sms_metrics = 1;
   }
-  int logn = 0;
-  while ((1 << logn) < n) ++logn;
   // grid: about one CTA per SM (fewer for small grids), a multiple of
-  // mult = n / 1024 when n > 1024 so that the stride (grid * 1024 points) is
-  // a multiple of n.
+  // mult = n / gcd(n, 1024) so that the stride (grid * 1024 points) is a
+  // multiple of n.
   const int n2 = n * n;
   const int want = (n2 + kThreads * kUnroll - 1) / (kThreads * kUnroll);
-  const int mult = n > kThreads ? n / kThreads : 1;
+  int g = n, b = kThreads;
+  while (b) {
+    const int r = g % b;
+    g = b;
+    b = r;
+  }
+  const int mult = n / g;
   int grid = want < g_sms_metrics ? want : g_sms_metrics;
   grid = grid / mult * mult;
   if (grid < mult) grid = mult;
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e = cudaMemsetAsync(moments, 0, 5 * sizeof(double), st);
   if (e == cudaSuccess) {
-    moments1_kernel<<<grid, kThreads, 0, st>>>(reinterpret_cast<const float2*>(field), logn,
+    moments1_kernel<<<grid, kThreads, 0, st>>>(reinterpret_cast<const float2*>(field), n,
                                                moments);
     e = cudaGetLastError();
   }
@@ -178,7 +184,7 @@ extern "C" lp_status lp_beam_moments(const lp_cfloat* field, int n, double* mome
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    e = cudaLaunchKernelEx(&cfg, moments2_kernel, reinterpret_cast<const float2*>(field), logn,
+    e = cudaLaunchKernelEx(&cfg, moments2_kernel, reinterpret_cast<const float2*>(field), n,
                            moments);
   }
   if (e != cudaSuccess)

@@ -110,7 +110,7 @@ extern "C" lp_status lp_plain_propagate_field_noalloc(const lp_cfloat* field_in,
                                                       lp_cfloat* field_out, int n,
                                                       double area_size, double wl, double z,
                                                       uint32_t flags, void* stream) {
-  if (!lp_is_supported_n(n) || n > kMaxN) {
+  if (!size_ops(n) || n > kMaxN) {
     char msg[160];
     snprintf(msg, sizeof(msg),
              "lp_plain_propagate_field_noalloc: npoints=%d unsupported (powers of two "

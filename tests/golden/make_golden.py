@@ -256,6 +256,24 @@ def main(ref_path):
         out[f"cfg2_{tag}_col"] = f[::16, 1024].copy()
         out[f"cfg2_{tag}_energy"] = np.array(np.sum(np.abs(f) ** 2))
 
+    # --- sizes that are not powers of two (the reference takes any npoints):
+    #     even 100 and odd 75; lens then propagate, a coordinate and a
+    #     spectral filter, the spectrum and iprofile.
+    for n, tag in ((100, "np100"), (75, "np75")):
+        V = lp.Beam2D(1 * lp.mm, n, 632 * lp.nm, init_field_gen=lp.gaussian_beam,
+                      init_gen_args=(1, 150 * lp.um))
+        out[f"{tag}_in"] = V.field.copy()
+        V.lens(5.0)
+        V.propagate(0.3)
+        out[f"{tag}_lens_prop_field"] = V.field.copy()
+        out[f"{tag}_lens_prop_spectrum"] = V.spectrum.copy()
+        V.coordinate_filter(f_gen=lp.round_hole, fargs=(300 * lp.um,))
+        V.spectral_filter(f_gen=lp.gaussian_beam, fargs=(1, 2e4))
+        V.propagate(0.5)
+        out[f"{tag}_filt_prop_field"] = V.field.copy()
+        out[f"{tag}_filt_prop_iprofile"] = V.iprofile.copy()
+        out[f"{tag}_z"] = np.array(V.z)
+
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     print("wrote", len(out), "arrays")
 

@@ -39,9 +39,11 @@ def test_every_declared_symbol_is_exported(lib):
 
 def test_meta_calls(lib):
     assert lib.lp_abi_version() == 1
-    for n in (16, 32, 64, 128, 256, 512, 1024, 2048, 4096, 8192):
+    # powers of two 16..8192 (the pass kernels) and any other n in 2..4096
+    # (Bluestein transforms)
+    for n in (2, 3, 8, 100, 75, 4095, 16, 32, 64, 128, 256, 512, 1024, 2048, 4096, 8192):
         assert lib.lp_is_supported_n(n) == 1
-    for n in (0, 8, 100, 16384, -4):
+    for n in (0, 1, 4097, 6000, 16384, -4):
         assert lib.lp_is_supported_n(n) == 0
     assert lib.lp_status_string(0) == b"ok"
 
@@ -50,9 +52,9 @@ def test_validation_before_any_device_call(lib):
     from lightprop2d_gb300 import _lib as L
     vp = ctypes.c_void_p
     # unsupported size: rejected before touching CUDA
-    st = lib.lp_fft2(vp(256), vp(256), 100, 0, vp(0))
+    st = lib.lp_fft2(vp(256), vp(256), 5000, 0, vp(0))
     assert st == L.LP_ERR_UNSUPPORTED_SIZE
-    assert b"npoints=100" in lib.lp_last_error()
+    assert b"npoints=5000" in lib.lp_last_error()
     # NULL pointer
     st = lib.lp_fft2(vp(0), vp(256), 64, 0, vp(0))
     assert st == L.LP_ERR_INVALID_ARGUMENT

@@ -152,7 +152,7 @@ def test_field_assignment_keeps_spectrum(lp):
 
 def test_unsupported_npoints(lp):
     with pytest.raises(ValueError):
-        lp.Beam2D(1 * mm, 100, 632 * nm, init_field=np.ones((100, 100)))
+        lp.Beam2D(1 * mm, 5000, 632 * nm, init_field=np.ones((1, 1)))
 
 
 def test_missing_init_raises(lp):

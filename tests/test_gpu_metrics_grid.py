@@ -139,7 +139,7 @@ def test_grid_errors(lp):
     with pytest.raises(ValueError):
         b.expand(0.5 * mm)
     with pytest.raises(ValueError):
-        b.expand(1.5 * mm)                 # 192 points: not a supported size
+        b.expand(40 * mm)                  # 5120 points: not a supported size
     with pytest.raises(ValueError):
         b.coarse(3)
     with pytest.raises(ValueError):

@@ -273,7 +273,7 @@ def ctypes_vp(v):
 
 def test_errors_are_raised(B):
     with pytest.raises(ValueError):
-        B.fft2(torch.zeros((100, 100), dtype=torch.complex64, device="cuda"))
+        B.fft2(torch.zeros((1, 1), dtype=torch.complex64, device="cuda"))  # npoints 1
     with pytest.raises(ValueError):
         B.fft2(torch.zeros((64, 64), dtype=torch.complex128, device="cuda"))
     with pytest.raises(ValueError):

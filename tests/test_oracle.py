@@ -183,3 +183,20 @@ def test_config2_2048_reference_run(golden):
             assert O.rel_l2(v, golden[f"cfg2_{tag}_{k}"]) < 1e-10, (tag, k)
         e = np.sum(np.abs(b.field) ** 2)
         assert abs(e - golden[f"cfg2_{tag}_energy"]) < 1e-10 * e
+
+
+@pytest.mark.parametrize("n,tag", [(100, "np100"), (75, "np75")])
+def test_sizes_not_powers_of_two(golden, n, tag):
+    """Even and odd npoints that are not powers of two: lens, propagate,
+    round-hole and Gaussian filters, against the reference's own run."""
+    b = O.OracleBeam(1 * mm, n, 632 * nm, init_field=golden[f"{tag}_in"])
+    b.lens(5.0)
+    b.propagate(0.3)
+    assert O.rel_l2(b.field, golden[f"{tag}_lens_prop_field"]) < TIGHT
+    assert O.rel_l2(b.spectrum, golden[f"{tag}_lens_prop_spectrum"]) < TIGHT
+    hole = np.exp(-(b.X ** 2 + b.Y ** 2) / (300 * um) ** 2) >= 1 / np.exp(0.5)
+    b.coordinate_filter(hole)
+    b.spectral_filter(np.exp(-(b.Kx ** 2 + b.Ky ** 2) / 2e4 ** 2))
+    b.propagate(0.5)
+    assert O.rel_l2(b.field, golden[f"{tag}_filt_prop_field"]) < TIGHT
+    assert np.allclose(b.iprofile, golden[f"{tag}_filt_prop_iprofile"], rtol=1e-10, atol=1e-14)
