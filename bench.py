@@ -432,6 +432,14 @@ class _Window:
         self.cs.windows.append((self.t0, time.time()))
 
 
+def B_c128_step(lib, fin, fout, n, sp):
+    """One complex128 fused propagate (Z) through the C ABI."""
+    nul = ctypes.c_void_p(0)
+    return lib.lp_propagate_field_c128(ctypes.c_void_p(fin.data_ptr()),
+                                       ctypes.c_void_p(fout.data_ptr()), nul, nul, n, AREA, WL,
+                                       Z, 0.0, nul, 0, nul, 0, 0, sp)
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -698,6 +706,19 @@ def main():
             sweep[str(nn)] = {"ms": round(ms, 5), "propagates_per_s": round(1e3 / ms, 1),
                               "effective_gbs": round(16 * nn * nn / (ms * 1e-3) / 1e9, 1)}
             del sl
+        # complex128 (complex_bits=128, the reference's default dtype): the
+        # FP64 family on the same workload, a few steps
+        z128_in = torch.as_tensor(O.gaussian(n, AREA, 1.0, WAIST), device=dev)
+        z128_out = torch.empty_like(z128_in)
+        with clocks.window():
+            zms, _ = timed(lambda i: B_c128_step(lib, z128_in, z128_out, n, sp), 10, 3)
+        _, z_ref = O.propagate(np.fft.fft2(O.gaussian(n, AREA, 1.0, WAIST)), g["Kz"], Z)
+        torch.cuda.synchronize()
+        extra["complex128_propagate"] = {
+            "ms": round(statistics.fmean(zms), 4),
+            "rel_l2_vs_fp64_oracle": O.rel_l2(z128_out.cpu().numpy(), z_ref),
+            "note": "lp_propagate_field_c128: FP64 transforms, float64 transfer function"}
+        del z128_in, z128_out
         st = statistics.fmean(st_ms)
         extra.update({
             "spectrum_state_propagate": {

@@ -42,6 +42,12 @@ typedef struct lp_cfloat {
   float im;
 } lp_cfloat;
 
+/* complex128, numpy / torch layout (re, im interleaved), 16-byte aligned. */
+typedef struct lp_cdouble {
+  double re;
+  double im;
+} lp_cdouble;
+
 typedef enum lp_status {
   LP_OK = 0,
   LP_ERR_INVALID_ARGUMENT = 1,  /* null pointer, bad dtype code, non-finite scalar */
@@ -77,7 +83,8 @@ typedef enum lp_mask_type {
    * (lightprop2d_gb300/generators.py), so boolean edges match it exactly. */
   LP_MASK_SEP_F32 = 7,
   LP_MASK_SPAN_I32 = 8,
-  LP_MASK_SEP_C64 = 9
+  LP_MASK_SEP_C64 = 9,
+  LP_MASK_SEP_C128 = 10   /* complex128 fx[N], fy[N] (the *_c128 entry points only) */
 } lp_mask_type;
 
 /* Flags (bitwise OR). */
@@ -185,6 +192,55 @@ lp_status lp_spectral_filter(lp_cfloat* spectrum, lp_cfloat* field_out, int n,
 
 /* Beam2D.iprofile (beam2d.py:717): out = |field|^2 as float32. */
 lp_status lp_iprofile(const lp_cfloat* field, float* out, int n, void* stream);
+
+/* ---- complex128 (complex_bits=128, the reference's default dtype,
+ * beam2d.py:88, :112-113) ----
+ * The same operations with complex128 grids (16-byte aligned), FP64
+ * transforms and the reference's float64 transfer function and lens phase
+ * (beam2d.py:305-308, :485-489, :508-510), so results agree with its numpy
+ * complex128 path to round-off.  Masks: any lp_mask_type (LP_MASK_SEP_C128
+ * included), promoted to complex128.  Flags: LP_FLAG_EVANESCENT_MASK, and
+ * LP_FLAG_SPECTRUM_READONLY for lp_propagate_c128.  npoints as for the
+ * complex64 entry points.  The first call of a size on a device builds
+ * tables (and, for sizes that are not powers of two, a per-stream work grid)
+ * and is refused inside stream capture (LP_ERR_NOT_INITIALIZED). */
+
+/* lp_fft2 in complex128 (beam2d.py:207-229). */
+lp_status lp_fft2_c128(const lp_cdouble* in, lp_cdouble* out, int n, int inverse,
+                       void* stream);
+
+/* Beam2D.propagate (beam2d.py:462-490) in complex128: spectrum *= H(z) *
+ * kmask (unless LP_FLAG_SPECTRUM_READONLY); field = ifft2(spectrum). */
+lp_status lp_propagate_c128(lp_cdouble* spectrum, lp_cdouble* field, int n, double area_size,
+                            double wl, double z, const void* kmask, int kmask_type,
+                            uint32_t flags, void* stream);
+
+/* lp_propagate_field in complex128: [lens, xmask] -> fft2 -> [kmask] * H(z)
+ * (spectrum_out optional) -> ifft2 -> iprofile_out (float64, optional). */
+lp_status lp_propagate_field_c128(const lp_cdouble* field_in, lp_cdouble* field_out,
+                                  lp_cdouble* spectrum_out, double* iprofile_out, int n,
+                                  double area_size, double wl, double z, double lens_f,
+                                  const void* xmask, int xmask_type, const void* kmask,
+                                  int kmask_type, uint32_t flags, void* stream);
+
+/* Beam2D.lens (beam2d.py:492-511) in complex128. */
+lp_status lp_lens_c128(lp_cdouble* field, lp_cdouble* spectrum_out, int n, double area_size,
+                       double wl, double f, void* stream);
+
+/* Beam2D.coordinate_filter (beam2d.py:310-342) in complex128. */
+lp_status lp_coordinate_filter_c128(lp_cdouble* field, lp_cdouble* spectrum_out, int n,
+                                    const void* mask, int mask_type, void* stream);
+
+/* Beam2D.spectral_filter (beam2d.py:344-373) in complex128. */
+lp_status lp_spectral_filter_c128(lp_cdouble* spectrum, lp_cdouble* field_out, int n,
+                                  const void* mask, int mask_type, void* stream);
+
+/* spectrum *= H(z) in complex128 (the propagate phase of beam2d.py:485-489). */
+lp_status lp_apply_transfer_c128(lp_cdouble* spectrum, int n, double area_size, double wl,
+                                 double z, uint32_t flags, void* stream);
+
+/* Beam2D.iprofile (beam2d.py:717) of a complex128 field: float64. */
+lp_status lp_iprofile_c128(const lp_cdouble* field, double* out, int n, void* stream);
 /* Intensity moments for Beam2D.centroid / D4sigma / centroid_intensity
  * (beam2d.py:669-752).  Writes 5 doubles to device memory `moments`, with
  * I = |field|^2, jx = ix - n/2, jy = iy - n/2 (grid-index offsets):

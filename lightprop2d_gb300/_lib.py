@@ -33,6 +33,7 @@ LP_MASK_C128 = 6
 LP_MASK_SEP_F32 = 7
 LP_MASK_SPAN_I32 = 8
 LP_MASK_SEP_C64 = 9
+LP_MASK_SEP_C128 = 10
 
 # flags
 LP_FLAG_PHASE_FP32 = 0x1
@@ -89,6 +90,15 @@ SIGNATURES = {
     "lp_modes_project": [_vp, _i, _i, _vp, _i, _vp, _vp],
     "lp_modes_combine": [_vp, _i, _i, _vp, _vp, _i, _vp],
     "lp_apply_transfer": [_vp, _i, _d, _d, _d, _u, _vp],
+    "lp_fft2_c128": [_vp, _vp, _i, _i, _vp],
+    "lp_propagate_c128": [_vp, _vp, _i, _d, _d, _d, _vp, _i, _u, _vp],
+    "lp_propagate_field_c128": [_vp, _vp, _vp, _vp, _i, _d, _d, _d, _d, _vp, _i, _vp, _i,
+                                _u, _vp],
+    "lp_lens_c128": [_vp, _vp, _i, _d, _d, _d, _vp],
+    "lp_coordinate_filter_c128": [_vp, _vp, _i, _vp, _i, _vp],
+    "lp_spectral_filter_c128": [_vp, _vp, _i, _vp, _i, _vp],
+    "lp_apply_transfer_c128": [_vp, _i, _d, _d, _d, _u, _vp],
+    "lp_iprofile_c128": [_vp, _vp, _i, _vp],
     "lp_plain_propagate_field": [_vp, _vp, _i, _d, _d, _d, _u, _vp],
     "lp_plain_propagate_field_noalloc": [_vp, _vp, _i, _d, _d, _d, _u, _vp],
     "lp_batch_create": [ctypes.POINTER(BeamDesc), _i, ctypes.POINTER(BatchOptions),

@@ -102,21 +102,28 @@ def is_supported(n: int) -> bool:
     return bool(L.load().lp_is_supported_n(int(n)))
 
 
+def _zgrid(t: torch.Tensor, name: str):
+    """(N, entry-point suffix) of a complex64 ("") or complex128 ("_c128") grid."""
+    if isinstance(t, torch.Tensor) and t.dtype == torch.complex128:
+        return _grid(t, name, torch.complex128), "_c128"
+    return _grid(t, name), ""
+
+
 def fft2(x: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
-    """numpy.fft.fft2 convention (beam2d.py:207-217)."""
-    n = _grid(x, "x")
+    """numpy.fft.fft2 convention (beam2d.py:207-217); complex64 or complex128."""
+    n, sfx = _zgrid(x, "x")
     out = torch.empty_like(x) if out is None else out
-    _grid(out, "out")
-    _call("lp_fft2", x.device, _vp(x), _vp(out), n, 0)
+    _grid(out, "out", x.dtype)
+    _call("lp_fft2" + sfx, x.device, _vp(x), _vp(out), n, 0)
     return out
 
 
 def ifft2(x: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
     """numpy.fft.ifft2 convention, 1/N^2 included (beam2d.py:219-229)."""
-    n = _grid(x, "x")
+    n, sfx = _zgrid(x, "x")
     out = torch.empty_like(x) if out is None else out
-    _grid(out, "out")
-    _call("lp_fft2", x.device, _vp(x), _vp(out), n, 1)
+    _grid(out, "out", x.dtype)
+    _call("lp_fft2" + sfx, x.device, _vp(x), _vp(out), n, 1)
     return out
 
 
@@ -125,13 +132,13 @@ def propagate(spectrum: torch.Tensor, area_size: float, wl: float, z: float,
               write_spectrum: bool = True, flags: int = 0) -> torch.Tensor:
     """Beam2D.propagate (beam2d.py:481-490): spectrum *= kmask*H(z) (in place
     unless ``write_spectrum=False``) and return field = ifft2(spectrum)."""
-    n = _grid(spectrum, "spectrum")
+    n, sfx = _zgrid(spectrum, "spectrum")
     field_out = torch.empty_like(spectrum) if field_out is None else field_out
-    _grid(field_out, "field_out")
+    _grid(field_out, "field_out", spectrum.dtype)
     km, kc = mask_arg(kmask, n, spectrum.device, "kmask")
     if not write_spectrum:
         flags |= L.LP_FLAG_SPECTRUM_READONLY
-    _call("lp_propagate", spectrum.device, _vp(spectrum), _vp(field_out), n,
+    _call("lp_propagate" + sfx, spectrum.device, _vp(spectrum), _vp(field_out), n,
           float(area_size), float(wl), float(z), _vp(km), kc, int(flags))
     return field_out
 
@@ -140,17 +147,18 @@ def propagate_field(field: torch.Tensor, area_size: float, wl: float, z: float,
                     out: torch.Tensor | None = None, spectrum_out=None,
                     iprofile_out=None, lens_f: float = 0.0, xmask=None,
                     xmask_phase: bool = False, kmask=None, flags: int = 0) -> torch.Tensor:
-    """Fused field -> field: [lens, xmask] -> fft2 -> [kmask] * H(z) -> ifft2."""
-    n = _grid(field, "field")
+    """Fused field -> field: [lens, xmask] -> fft2 -> [kmask] * H(z) -> ifft2.
+    complex128 fields run the FP64 family (iprofile_out float64)."""
+    n, sfx = _zgrid(field, "field")
     out = torch.empty_like(field) if out is None else out
-    _grid(out, "out")
+    _grid(out, "out", field.dtype)
     if spectrum_out is not None:
-        _grid(spectrum_out, "spectrum_out")
+        _grid(spectrum_out, "spectrum_out", field.dtype)
     if iprofile_out is not None:
-        _grid(iprofile_out, "iprofile_out", torch.float32)
+        _grid(iprofile_out, "iprofile_out", torch.float64 if sfx else torch.float32)
     xm, xc = mask_arg(xmask, n, field.device, "xmask", phase=xmask_phase)
     km, kc = mask_arg(kmask, n, field.device, "kmask")
-    _call("lp_propagate_field", field.device, _vp(field), _vp(out), _vp(spectrum_out),
+    _call("lp_propagate_field" + sfx, field.device, _vp(field), _vp(out), _vp(spectrum_out),
           _vp(iprofile_out), n, float(area_size), float(wl), float(z), float(lens_f),
           _vp(xm), xc, _vp(km), kc, int(flags))
     return out
@@ -159,37 +167,38 @@ def propagate_field(field: torch.Tensor, area_size: float, wl: float, z: float,
 def lens(field: torch.Tensor, area_size: float, wl: float, f: float,
          spectrum_out: torch.Tensor | None = None) -> None:
     """Beam2D.lens (beam2d.py:508-511) in place; optional spectrum = fft2(field)."""
-    n = _grid(field, "field")
+    n, sfx = _zgrid(field, "field")
     if spectrum_out is not None:
-        _grid(spectrum_out, "spectrum_out")
-    _call("lp_lens", field.device, _vp(field), _vp(spectrum_out), n, float(area_size),
+        _grid(spectrum_out, "spectrum_out", field.dtype)
+    _call("lp_lens" + sfx, field.device, _vp(field), _vp(spectrum_out), n, float(area_size),
           float(wl), float(f))
 
 
 def coordinate_filter(field: torch.Tensor, mask, spectrum_out=None, phase=False) -> None:
     """Beam2D.coordinate_filter(f_init=mask) (beam2d.py:339-342) in place."""
-    n = _grid(field, "field")
+    n, sfx = _zgrid(field, "field")
     if spectrum_out is not None:
-        _grid(spectrum_out, "spectrum_out")
+        _grid(spectrum_out, "spectrum_out", field.dtype)
     m, c = mask_arg(mask, n, field.device, "mask", phase=phase)
-    _call("lp_coordinate_filter", field.device, _vp(field), _vp(spectrum_out), n, _vp(m), c)
+    _call("lp_coordinate_filter" + sfx, field.device, _vp(field), _vp(spectrum_out), n, _vp(m), c)
 
 
 def spectral_filter(spectrum: torch.Tensor, mask, field_out=None) -> torch.Tensor:
     """Beam2D.spectral_filter(f_init=mask) (beam2d.py:370-373)."""
-    n = _grid(spectrum, "spectrum")
+    n, sfx = _zgrid(spectrum, "spectrum")
     field_out = torch.empty_like(spectrum) if field_out is None else field_out
     m, c = mask_arg(mask, n, spectrum.device, "mask")
-    _call("lp_spectral_filter", spectrum.device, _vp(spectrum), _vp(field_out), n, _vp(m), c)
+    _call("lp_spectral_filter" + sfx, spectrum.device, _vp(spectrum), _vp(field_out), n, _vp(m), c)
     return field_out
 
 
 def iprofile(field: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
-    """|field|^2 as float32 (beam2d.py:717)."""
-    n = _grid(field, "field")
-    out = torch.empty((n, n), dtype=torch.float32, device=field.device) if out is None else out
-    _grid(out, "out", torch.float32)
-    _call("lp_iprofile", field.device, _vp(field), _vp(out), n)
+    """|field|^2 as float32 (float64 for a complex128 field) (beam2d.py:717)."""
+    n, sfx = _zgrid(field, "field")
+    dt = torch.float64 if sfx else torch.float32
+    out = torch.empty((n, n), dtype=dt, device=field.device) if out is None else out
+    _grid(out, "out", dt)
+    _call("lp_iprofile" + sfx, field.device, _vp(field), _vp(out), n)
     return out
 
 
@@ -279,8 +288,8 @@ def crop(field: torch.Tensor, first: int, n_keep: int, x0: float, dL_in: float, 
 def apply_transfer(spectrum: torch.Tensor, area_size: float, wl: float, z: float,
                    flags: int = 0) -> None:
     """spectrum *= H(z) in place."""
-    n = _grid(spectrum, "spectrum")
-    _call("lp_apply_transfer", spectrum.device, _vp(spectrum), n, float(area_size),
+    n, sfx = _zgrid(spectrum, "spectrum")
+    _call("lp_apply_transfer" + sfx, spectrum.device, _vp(spectrum), n, float(area_size),
           float(wl), float(z), int(flags))
 
 

@@ -8,7 +8,8 @@ Same dataclass fields, methods and results as the reference class
 
 How the state is kept (observable results are the reference's):
 
-* ``field`` is a ``torch.complex64`` CUDA tensor.  Each operation that
+* ``field`` is a CUDA tensor of ``complex`` (complex128 for
+  ``complex_bits=128``, the reference's default, else complex64).  Each operation that
   replaces the field allocates a new tensor, as the reference rebinds
   ``self.field``.
 * The spectrum is state (beam2d.py:489).  It is stored as a base grid plus a
@@ -27,18 +28,20 @@ How the state is kept (observable results are the reference's):
 
 Differences, by design:
 
-* Storage is complex64 whatever ``complex_bits`` says (the kernels compute
-  in complex64 with FP64-grade transfer phases; results agree with the
-  reference's complex128 path to ~1e-6 relative L2).  ``complex_bits=128``
-  issues one warning.
+* ``complex_bits=128`` runs the propagation path (transforms, propagate,
+  lens, filters, iprofile) in the FP64 kernel family and agrees with the
+  reference's complex128 path to round-off; ``complex_bits=64`` runs the
+  fused complex64 kernels (FP64-grade transfer phases, ~1e-7 relative L2).
+  Beam metrics, grid management and mode decomposition compute in complex64
+  for either (results cast back to the beam's dtype).
 * ``use_gpu`` is accepted for signature compatibility; the backend always
   runs on a CUDA device.  ``numpy_output`` works as in the reference.
-* Supported ``npoints``: powers of two from 16 to 8192 (ValueError otherwise).
+* Supported ``npoints``: any from 2 to 4096, and powers of two up to 8192
+  (ValueError otherwise).
 """
 from __future__ import annotations
 
 import math
-import warnings
 from collections.abc import Iterable
 from dataclasses import dataclass
 from typing import Callable, Union
@@ -56,7 +59,6 @@ mm = 1e-1
 cm = 1
 m = 100
 
-_warned_c128 = False
 
 
 def _to_device(a, device, dtype=torch.complex64) -> torch.Tensor:
@@ -95,7 +97,6 @@ class Beam2D:
 
     # ------------------------------------------------------------ set-up --
     def __post_init__(self):
-        global _warned_c128
         self.xp = torch
         if self.device is None:
             self.device = torch.device("cuda", torch.cuda.current_device())
@@ -106,11 +107,12 @@ class Beam2D:
             raise ValueError(
                 f"npoints={self.npoints} is not supported by the GB300 backend "
                 "(powers of two from 16 to 8192)")
-        if self.complex_bits == 128 and not _warned_c128:
-            _warned_c128 = True
-            warnings.warn("complex_bits=128: the GB300 backend stores complex64 fields "
-                          "(transfer phases are evaluated to FP64-grade accuracy)")
-        self.complex = torch.complex64
+        if self.complex_bits == 64:
+            self.complex = torch.complex64
+        elif self.complex_bits == 128:
+            self.complex = torch.complex128
+        else:
+            raise ValueError("complex_bits must be 64 or 128")
         B.init(self.device)
         self._construct_grids()
         if self.init_field_gen is not None:
@@ -121,14 +123,14 @@ class Beam2D:
             raise ValueError(
                 "Init field data is None : " +
                 "'init_field_gen' must be a function or 'init_field' must be an array.")
-        self._field = _to_device(f, self.device)
+        self._field = _to_device(f, self.device, self.complex)
         self._check_grid(self._field, "init field")
         self._pend_invf = 0.0   # pending lens: sum of 1/f
         self._pend_xmask = None  # pending coordinate mask (device tensor)
         if self.init_spectrum is None:
             self._spec = None    # derived: fft2(field)
         else:
-            self._spec = _to_device(self.init_spectrum, self.device)
+            self._spec = _to_device(self.init_spectrum, self.device, self.complex)
             self._check_grid(self._spec, "init spectrum")
         self._spec_dz = 0.0
 
@@ -157,6 +159,10 @@ class Beam2D:
         return self._Kz
 
     # -------------------------------------------------------------- state --
+    def _c64(self, t):
+        """The complex64 view that the metrics, grid and mode kernels take."""
+        return t if t.dtype == torch.complex64 else t.to(torch.complex64)
+
     def _has_pending(self) -> bool:
         return self._pend_invf != 0.0 or self._pend_xmask is not None
 
@@ -185,7 +191,7 @@ class Beam2D:
             self._materialise_spectrum()
         self._pend_invf = 0.0
         self._pend_xmask = None
-        self._field = _to_device(value, self.device)
+        self._field = _to_device(value, self.device, self.complex)
         self._check_grid(self._field, "field")
 
     def _materialise_spectrum(self):
@@ -206,7 +212,7 @@ class Beam2D:
 
     @spectrum.setter
     def spectrum(self, value):
-        self._spec = _to_device(value, self.device)
+        self._spec = _to_device(value, self.device, self.complex)
         self._check_grid(self._spec, "spectrum")
         self._spec_dz = 0.0
 
@@ -216,8 +222,8 @@ class Beam2D:
         self.z = 0
         self._pend_invf = 0.0
         self._pend_xmask = None
-        self._field = _to_device(field, self.device)
-        self._spec = None if spectrum is None else _to_device(spectrum, self.device)
+        self._field = _to_device(field, self.device, self.complex)
+        self._spec = None if spectrum is None else _to_device(spectrum, self.device, self.complex)
         self._spec_dz = 0.0
 
     def propagate(self, z: float):
@@ -258,7 +264,7 @@ class Beam2D:
             X = torch.as_tensor(self.X, dtype=torch.float64, device=self.device)
             ph = torch.remainder((X[None, :] ** 2 + X[:, None] ** 2) * (self.k0 / (2 * f)),
                                  2 * math.pi)
-            self.coordinate_filter(f_init=torch.polar(torch.ones_like(ph), ph).to(torch.complex64))
+            self.coordinate_filter(f_init=torch.polar(torch.ones_like(ph), ph).to(self.complex))
             return
         self._pend_invf += self._xscale ** 2 / f  # the phase follows the (scaled) grid X
         self._spec = None
@@ -283,8 +289,9 @@ class Beam2D:
         """field *= f_gen(X, Y, *fargs) * f_init; spectrum = fft2(field)
         (beam2d.py:310-342)."""
         m = None
-        if f_init is None and f_gen is not None:
+        if f_init is None and f_gen is not None and self.complex == torch.complex64:
             # deterministic generators become a 2N table evaluated in the pass
+            # (complex128 beams keep the generator's float64 mask)
             m = G.compact(f_gen, fargs, self.X, self.Y, self.device)
         if m is None:
             m = self._mask(f_init, f_gen, fargs, self.X, self.Y)
@@ -303,7 +310,7 @@ class Beam2D:
         """spectrum *= f_gen(Kx, Ky, *fargs) * f_init; field = ifft2(spectrum)
         (beam2d.py:344-373)."""
         m = None
-        if f_init is None and f_gen is not None:
+        if f_init is None and f_gen is not None and self.complex == torch.complex64:
             m = G.compact(f_gen, fargs, self.Kx, self.Ky, self.device, allow_span=False)
         if m is None:
             m = self._mask(f_init, f_gen, fargs, self.Kx, self.Ky)
@@ -339,7 +346,7 @@ class Beam2D:
     def _moments(self):
         """(m0, m1, m2, m3, m4) of lp_beam_moments on the host; the reference's
         np.average raises ZeroDivisionError for a zero field, so does this."""
-        m = B.beam_moments(self.field).cpu().tolist()
+        m = B.beam_moments(self._c64(self.field)).cpu().tolist()
         if not m[0] > 0:
             raise ZeroDivisionError("Weights sum to zero, can't be normalized")
         return m
@@ -370,7 +377,7 @@ class Beam2D:
     def _regrid(self, field):
         """Swap in a field on the new grid; the spectrum is fft2(field), made
         when read (the reference computes it eagerly)."""
-        self._field = field
+        self._field = field.to(self.complex)
         self._pend_invf = 0.0
         self._pend_xmask = None
         self._spec = None
@@ -390,7 +397,7 @@ class Beam2D:
         if n < old:
             raise ValueError("expand: the new area must not be smaller than the current one")
         self._check_new_n(n, "expand")
-        f = B.expand(self.field, n)
+        f = B.expand(self._c64(self.field), n)
         self.npoints = n
         self.area_size = area_size
         self._construct_grids()
@@ -409,7 +416,7 @@ class Beam2D:
         x0, dL_in = float(self.X[first]), self.dL
         new_n = npoints if npoints else self.npoints
         self._check_new_n(new_n, "crop")
-        f = self.field
+        f = self._c64(self.field)
         self.npoints = new_n
         self.area_size = area_size
         self._construct_grids()
@@ -422,7 +429,7 @@ class Beam2D:
             raise ValueError(f"coarse: mean_order={mean_order} must divide npoints={self.npoints}")
         n = self.npoints // mean_order
         self._check_new_n(n, "coarse")
-        f = B.coarse(self.field, mean_order)
+        f = B.coarse(self._c64(self.field), mean_order)
         self.npoints = n
         self._construct_grids()
         self._regrid(f)
@@ -445,7 +452,7 @@ class Beam2D:
         n = self.npoints
         dL_in = float(self.X[1] - self.X[0])
         x0 = float(self.X[0]) - (abs(s) * dL_in if s < 0 else 0.0)
-        g = B.crop(self.field, 0, n, x0, dL_in, n, abs(s) * dL_in)
+        g = B.crop(self._c64(self.field), 0, n, x0, dL_in, n, abs(s) * dL_in)
         g *= s
         self._regrid(g)
         # phase = -(X^2+Y^2)*k0*(l1+l2)/(2*l2^2): a lens of focal length
@@ -467,16 +474,17 @@ class Beam2D:
         ``ModeBasis`` (uploaded once) or a list / array of flattened modes."""
         basis = M.ModeBasis(modes_list, self.device)
         if mode == "scalar":
-            c = M.project(basis, self.field)
+            c = M.project(basis, self._c64(self.field))
         elif mode == "lstsq":
-            c = M.lstsq(basis, self.field)
+            c = M.lstsq(basis, self._c64(self.field))
         else:
             raise ValueError(f"unknown mode {mode!r}: 'scalar' or 'lstsq'")
         return self._coeffs_out(c)
 
     def fast_deconstruct_by_modes(self, modes_matrix_t, modes_matrix_dot_t):
         """lstsq(modes_matrix_dot_t, modes_matrix_t . window) (beam2d.py:602-648)."""
-        return self._coeffs_out(M.fast_lstsq(modes_matrix_t, modes_matrix_dot_t, self.field))
+        return self._coeffs_out(M.fast_lstsq(modes_matrix_t, modes_matrix_dot_t,
+                                             self._c64(self.field)))
 
     def construct_by_modes(self, modes_list, modes_coeffs):
         """field = sum_i c_i * mode_i, zero outside the modes' window; the

@@ -1,0 +1,92 @@
+"""GPU: the complex128 family (complex_bits=128, the reference's default
+dtype) against numpy complex128 and the reference's own complex128 runs, to
+round-off (relative L2 <= 1e-11).  The complex64 goldens of
+test_gpu_beam2d.py run in both dtypes; this file adds the transforms, the
+fused propagate with every multiplier, config 2 at 2048^2 and the argument
+checks of the *_c128 entry points."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import lp_oracle as O
+
+pytestmark = pytest.mark.gpu
+um, nm, mm = O.um, O.nm, O.mm
+TOL128 = 1e-11
+
+
+def H(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def _rand(n, seed):
+    rng = np.random.default_rng(seed)
+    return rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+
+
+@pytest.mark.parametrize("n", [2, 8, 16, 64, 75, 100, 512, 1024, 2048])
+def test_fft2_c128(n):
+    from lightprop2d_gb300 import backend as B
+    x = _rand(n, n)
+    t = torch.as_tensor(x, device="cuda")
+    f = B.fft2(t)
+    assert f.dtype == torch.complex128
+    assert O.rel_l2(H(f), np.fft.fft2(x)) < TOL128
+    assert O.rel_l2(H(B.ifft2(f)), x) < TOL128
+
+
+@pytest.mark.parametrize("n,area,z", [(256, 0.05, 0.7), (100, 0.03, 0.2), (1024, 0.2, 3.0)])
+def test_propagate_field_c128_with_every_multiplier(n, area, z):
+    from lightprop2d_gb300 import backend as B
+    wl = 632 * nm
+    x = _rand(n, 2 * n)
+    rng = np.random.default_rng(1)
+    xm = rng.uniform(0.5, 1.0, size=(n, n))                      # float64 mask
+    km = np.exp(2j * np.pi * rng.uniform(size=(n, n)))           # complex128 mask
+    g = O.grids(area, n, wl)
+    xr = x * O.lens_phase(g["X"], g["Y"], g["k0"], 7.0) * xm
+    spec_z, want = O.propagate(O.fft2(xr) * km, g["Kz"], z)
+    t = torch.as_tensor(x, device="cuda")
+    s_out = torch.empty_like(t)
+    ip = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    got = B.propagate_field(t, area, wl, z, spectrum_out=s_out, iprofile_out=ip, lens_f=7.0,
+                            xmask=torch.as_tensor(xm, device="cuda"),
+                            kmask=torch.as_tensor(km, device="cuda"))
+    assert O.rel_l2(H(got), want) < TOL128
+    assert O.rel_l2(H(s_out), spec_z) < TOL128
+    assert np.linalg.norm(H(ip) - np.abs(want) ** 2) / np.linalg.norm(np.abs(want) ** 2) < TOL128
+
+
+def test_config2_2048_c128_against_the_reference_run(golden):
+    import lightprop2d_gb300 as lp
+    b = lp.Beam2D(2 * mm, 2048, 632 * nm, init_field_gen=lp.gaussian_beam,
+                  init_gen_args=(1, 100 * um))      # complex_bits=128, the default
+    assert b.field.dtype == torch.complex128
+    for tag, dz in (("z1", 1.0), ("z10", 9.0)):
+        b.propagate(dz)
+        f = H(b.field)
+        parts = {"window": f[992:1056, 992:1056], "row": f[1024, ::16], "col": f[::16, 1024]}
+        for k, v in parts.items():
+            assert O.rel_l2(v, golden[f"cfg2_{tag}_{k}"]) < 1e-10, (tag, k)
+        e = float(np.sum(np.abs(f) ** 2))
+        assert abs(e - float(golden[f"cfg2_{tag}_energy"])) < 1e-11 * e
+    ip = b.iprofile
+    assert ip.dtype == np.float64
+
+
+def test_c128_argument_checks():
+    from lightprop2d_gb300 import _lib as L
+    lib = L.load()
+    vp = ctypes.c_void_p
+    x = torch.zeros((64, 64), dtype=torch.complex128, device="cuda")
+    st = vp(torch.cuda.current_stream().cuda_stream)
+    assert lib.lp_fft2_c128(vp(x.data_ptr()), vp(x.data_ptr()), 5000, 0, st) == \
+        L.LP_ERR_UNSUPPORTED_SIZE
+    assert lib.lp_fft2_c128(vp(x.data_ptr() + 8), vp(x.data_ptr()), 64, 0, st) == \
+        L.LP_ERR_MISALIGNED
+    assert lib.lp_propagate_field_c128(vp(x.data_ptr()), vp(x.data_ptr()), vp(0), vp(0), 64,
+                                       0.1, 632e-7, 1.0, 0.0, vp(0), 0, vp(0), 0,
+                                       L.LP_FLAG_ADJOINT, st) == L.LP_ERR_INVALID_ARGUMENT

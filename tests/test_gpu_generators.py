@@ -39,7 +39,7 @@ def test_coordinate_filter_generators_fused(lp, n):
     x = O.random_phase_hole(n, A, 0.45 * A, seed=n)
     g = O.grids(A, n, wl)
     for f, args in cases(lp, A):
-        b = lp.Beam2D(A, n, wl, init_field=x)
+        b = lp.Beam2D(A, n, wl, init_field=x, complex_bits=64)
         Xr = b.X.copy()
         Yr = Xr.reshape((-1, 1))          # aliases Xr, as Beam2D's Y aliases X
         mask = np.broadcast_to(f(Xr, Yr, *args), (n, n))
@@ -51,7 +51,7 @@ def test_coordinate_filter_generators_fused(lp, n):
         _, ref = O.propagate(np.fft.fft2(fl), g["Kz"], z)
         assert O.rel_l2(H(b.field), ref) < TOL, f.__name__
         # and without a propagate: the field itself
-        c = lp.Beam2D(A, n, wl, init_field=x)
+        c = lp.Beam2D(A, n, wl, init_field=x, complex_bits=64)
         c.coordinate_filter(f_gen=f, fargs=args)
         assert O.rel_l2(H(c.field), fl) < 1e-6, f.__name__
 
@@ -63,14 +63,14 @@ def test_spectral_filter_generators_fused(lp):
     g = O.grids(A, n, wl)
     for f, args in [(lp.rectangle_hole, (900.0, 600.0)), (lp.gaussian_beam, (1.0, 800.0)),
                     (lp.square_slits, (150.0, 700.0))]:
-        b = lp.Beam2D(A, n, wl, init_field=x)
+        b = lp.Beam2D(A, n, wl, init_field=x, complex_bits=64)
         Kx = b.Kx.copy()
         m = np.broadcast_to(f(Kx, Kx.reshape((-1, 1)), *args), (n, n))
         b.spectral_filter(f_gen=f, fargs=args)
         ref = np.fft.ifft2(np.fft.fft2(x.astype(np.complex64)) * m)
         assert O.rel_l2(H(b.field), ref) < TOL, f.__name__
     # round_hole on the K grid is not row-interval shaped: host mask path
-    b = lp.Beam2D(A, n, wl, init_field=x)
+    b = lp.Beam2D(A, n, wl, init_field=x, complex_bits=64)
     b.spectral_filter(f_gen=lp.round_hole, fargs=(700.0,))
     m = lp.round_hole(b.Kx.copy(), b.Kx.copy().reshape((-1, 1)), 700.0)
     assert O.rel_l2(H(b.field), np.fft.ifft2(np.fft.fft2(x.astype(np.complex64)) * m)) < TOL
