@@ -169,12 +169,15 @@ def batch_workload(dev, seed=3, mix=BATCH_MIX, scale=1.0):
     return out
 
 
-def batch_section(dev, stream, clocks, reps, check_oracle=True, scale=1.0, compare=True):
+def batch_section(dev, stream, clocks, reps, check_oracle=True, scale=1.0, compare=True,
+                  shard_of=None):
     """Config: the uneven batch as one persistent launch in a CUDA graph
     (autotuned options), against the same beams as per-beam fused calls.
     Parity: sampled beams against the oracle, and for every beam energy
     conservation (the lens and H are unimodular: sum |u|^2 before equals
-    sum of the iprofile after, to FFT round-off)."""
+    sum of the iprofile after, to FFT round-off).  shard_of = (world, rank):
+    only this rank's share of the beams (batch.shard: points balanced, no
+    collective), as a multi-GPU run splits the batch."""
     import torch
     from lightprop2d_gb300 import _lib as L
     from lightprop2d_gb300 import backend as B
@@ -183,11 +186,18 @@ def batch_section(dev, stream, clocks, reps, check_oracle=True, scale=1.0, compa
     from oracle import lp_oracle as O
 
     W = batch_workload(dev, scale=scale)
-    nb, pts = len(W["fields"]), sum(n * n for n in W["n"])
     e_in = torch.cat([(st.real ** 2 + st.imag ** 2).sum((1, 2), dtype=torch.float64)
                       for st, _ in W["stacks"]])
+    own = None
+    if shard_of is not None:
+        from lightprop2d_gb300.batch import shard
+        own = shard(W["n"], *shard_of)
+        for k in ("fields", "iprofiles", "area", "z", "f", "n"):
+            W[k] = [W[k][i] for i in own]
+        e_in = e_in[torch.as_tensor(own, device=e_in.device)]
+    nb, pts = len(W["fields"]), sum(n * n for n in W["n"])
     # parity sample: first beam of every size, kept on the host before any run
-    pick = [W["n"].index(n) for n, _ in BATCH_MIX]
+    pick = [W["n"].index(n) for n, _ in BATCH_MIX if n in W["n"]]
     keep = {i: W["fields"][i].cpu().numpy() for i in pick}
     args = (W["area"], BATCH_WL, W["z"], W["f"], W["iprofiles"])
     bb = BeamBatch(W["fields"], *args)
@@ -203,6 +213,8 @@ def batch_section(dev, stream, clocks, reps, check_oracle=True, scale=1.0, compa
             _, x = O.propagate(O.fft2(x), g["Kz"], W["z"][i])
             errs[str(n)] = O.rel_l2(W["fields"][i].cpu().numpy(), x)
     e_out = torch.cat([ip.sum((1, 2), dtype=torch.float64) for _, ip in W["stacks"]])
+    if own is not None:
+        e_out = e_out[torch.as_tensor(own, device=e_out.device)]
     energy_err = float(((e_out - e_in).abs() / e_in).max())
     bb.close()
     del keep
@@ -244,6 +256,7 @@ def batch_section(dev, stream, clocks, reps, check_oracle=True, scale=1.0, compa
         bb.close()
         del graph
         return {"beams": nb, "points": pts, "ms_per_batch": round(t_graph, 4),
+                "ms_per_batch_with_moments": round(t_moments, 4), "plan": info,
                 "energy_rel_err_max_all_beams": energy_err, "rel_l2_vs_fp64_oracle": errs}
 
     # the same beams as one fused field->field call each (3 launches per beam)
@@ -458,6 +471,16 @@ def main():
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
         return run_reference(args)
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # --gpus N without a launcher: start N ranks (one per GPU) on this node
+        import socket
+        with socket.socket() as sk:
+            sk.bind(("127.0.0.1", 0))
+            port = sk.getsockname()[1]
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+               f"--nproc-per-node={args.gpus}", "--master-addr=127.0.0.1",
+               f"--master-port={port}", os.path.abspath(__file__)] + sys.argv[1:]
+        return subprocess.call(cmd)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -791,12 +814,38 @@ def main():
         torch.cuda.empty_cache()
 
         # Uneven batch: 4096 beams in one persistent launch (CUDA graph).
-        extra["batch_uneven"] = batch_section(dev, stream, clocks, reps=20)
-        torch.cuda.empty_cache()
+        if world == 1:
+            extra["batch_uneven"] = batch_section(dev, stream, clocks, reps=20)
+            torch.cuda.empty_cache()
 
         # Metrics, generators, grid management, mode decomposition.
         with clocks.window():
             extra["next_rows"] = next_rows_section(dev, stream, hbm)
+        torch.cuda.empty_cache()
+
+    # ------------------------------------------ uneven batch, sharded (N > 1) --
+    # Every rank runs its share of the 4096 beams (batch.shard: points
+    # balanced, no collective on the data path) as one graph-replayed launch;
+    # the batch takes as long as the slowest rank.
+    if world > 1 and not args.quick:
+        ranks_in_step["on"] = True
+        dist.barrier()
+        mine = batch_section(dev, stream, clocks, reps=20, check_oracle=(rank == 0),
+                             compare=False, shard_of=(world, rank))
+        per = [None] * world
+        dist.all_gather_object(per, {"rank": rank, **mine})
+        t_max = max(r["ms_per_batch"] for r in per)
+        nb_all = sum(r["beams"] for r in per)
+        extra["batch_uneven"] = {
+            "workload": "4096 beams: " + ", ".join(f"{c} x {n}^2" for n, c in BATCH_MIX)
+                        + ", hole+lens+propagate+iprofile, wl 632 nm; sharded over ranks",
+            "ranks": world, "beams": nb_all, "ms_per_batch": round(t_max, 4),
+            "beams_per_s": round(nb_all / (t_max * 1e-3), 1),
+            "points_per_s": round(sum(r["points"] for r in per) / (t_max * 1e-3), 1),
+            "per_rank": [{k: r[k] for k in ("rank", "beams", "points", "ms_per_batch")}
+                         for r in per],
+            "rel_l2_vs_fp64_oracle_rank0": per[0]["rel_l2_vs_fp64_oracle"],
+            "energy_rel_err_max": max(r["energy_rel_err_max_all_beams"] for r in per)}
         torch.cuda.empty_cache()
 
     # ----------------------------------------------------------------- e2e --

@@ -359,6 +359,14 @@ lp_status lp_batch_status(lp_batch* batch, void* stream);
 /* Queue and launch shape: items, CTAs launched, resident CTAs per SM. */
 lp_status lp_batch_info(const lp_batch* batch, int* n_items, int* grid,
                         int* ctas_per_sm);
+
+/* The host part of lp_batch_create alone: checks the beams and builds the
+ * work queue, with no CUDA call, so a rank can plan its shard of a beam list
+ * (see batch.partition_beams) on any host.  Returns the number of queue
+ * items, tiles and grid points of the plan.  No reference counterpart. */
+lp_status lp_batch_plan(const lp_beam_desc* beams, int count,
+                        const lp_batch_options* options, int* n_items,
+                        long long* n_tiles, long long* n_points);
 lp_status lp_batch_destroy(lp_batch* batch);
 
 /* -------------------------------------------------- unfused comparison --

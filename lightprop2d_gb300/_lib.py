@@ -106,6 +106,9 @@ SIGNATURES = {
     "lp_batch_run": [_vp, _vp],
     "lp_batch_status": [_vp, _vp],
     "lp_batch_info": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(_i)],
+    "lp_batch_plan": [ctypes.POINTER(BeamDesc), _i, ctypes.POINTER(BatchOptions),
+                      ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_longlong),
+                      ctypes.POINTER(ctypes.c_longlong)],
     "lp_batch_destroy": [_vp],
 }
 _RESTYPES = {"lp_last_error": ctypes.c_char_p, "lp_status_string": ctypes.c_char_p}

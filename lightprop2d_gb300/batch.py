@@ -136,6 +136,37 @@ class BeamBatch:
             pass
 
 
+def plan_info(sizes: Sequence[int], area_size, wl, z, lens_f=0.0, flags: int = 0,
+              tiles_per_item: int = 0, group_points_log2: int = 0) -> dict:
+    """The work queue lp_batch_create would build for beams of these grid
+    sizes (host only, no CUDA call: lp_batch_plan).  Field pointers are
+    placeholders; only the plan is computed.  Returns items, tiles, points."""
+    nb = len(sizes)
+    if nb == 0:
+        raise ValueError("empty batch")
+
+    def per(v):
+        return [float(x) for x in v] if isinstance(v, (list, tuple)) else [float(v)] * nb
+    areas, wls, zs, fs = per(area_size), per(wl), per(z), per(lens_f)
+    descs = (L.BeamDesc * nb)()
+    for i, n in enumerate(sizes):
+        # placeholder addresses: aligned, never dereferenced by the planner
+        descs[i] = L.BeamDesc(4096 * (i + 1), 0, int(n), areas[i], wls[i], zs[i], fs[i],
+                              int(flags), 0)
+    opts = L.BatchOptions(0, int(tiles_per_item), int(group_points_log2), 0, 0)
+    items, tiles, points = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_longlong()
+    L.check(L.load().lp_batch_plan(descs, nb, ctypes.byref(opts), ctypes.byref(items),
+                                   ctypes.byref(tiles), ctypes.byref(points)), "lp_batch_plan")
+    return {"items": items.value, "tiles": tiles.value, "points": points.value}
+
+
+def shard(sizes: Sequence[int], world: int, rank: int) -> list[int]:
+    """The beam indices rank `rank` of `world` propagates (partition_beams)."""
+    if not 0 <= rank < world:
+        raise ValueError("rank out of range")
+    return partition_beams(sizes, world)[rank]
+
+
 def partition_beams(sizes: Sequence[int], world: int) -> list[list[int]]:
     """Split beams (grid sizes n) over `world` ranks, balancing points:
     longest-processing-time greedy (largest beam to the lightest rank).

@@ -233,14 +233,16 @@ struct lp_batch {
   BatchPlan plan;
 };
 
-extern "C" {
+namespace {
 
-lp_status lp_batch_create(const lp_beam_desc* beams, int count, const lp_batch_options* options,
-                          lp_batch** out) {
-  if (!out) return fail(LP_ERR_INVALID_ARGUMENT, "lp_batch_create: out is NULL");
-  *out = nullptr;
+// Host part of a batch: argument checks, per-beam records (largest beams
+// first) and the work queue.  No CUDA call, so it also plans shards on hosts
+// without a GPU (lp_batch_plan).
+lp_status plan_batch(const lp_beam_desc* beams, int count, const lp_batch_options* options,
+                     std::vector<BeamRec>& recs, std::vector<Item>& items,
+                     lp_batch_options& opt) {
   if (!beams || count <= 0) return fail(LP_ERR_INVALID_ARGUMENT, "lp_batch_create: no beams");
-  lp_batch_options opt = {};
+  opt = lp_batch_options{};
   if (options) opt = *options;
   const int tpi = opt.tiles_per_item > 0 ? opt.tiles_per_item : 8;
   const int glog = opt.group_points_log2 > 0 ? opt.group_points_log2 : 23;
@@ -265,18 +267,12 @@ lp_status lp_batch_create(const lp_beam_desc* beams, int count, const lp_batch_o
       return fail(LP_ERR_INVALID_ARGUMENT,
                   "beam flags: only LP_FLAG_PHASE_FP32 and LP_FLAG_EVANESCENT_MASK apply");
   }
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-  lp_status s = lp_init(dev);
-  if (s != LP_OK) return s;
-
   // Host records: beams sorted by size (largest first).
   std::vector<int> order(count);
   for (int i = 0; i < count; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int b) { return beams[a].n > beams[b].n; });
-  std::vector<BeamRec> recs(count);
+  recs.assign(count, BeamRec{});
   for (int k = 0; k < count; ++k) {
     const lp_beam_desc& b = beams[order[k]];
     BeamRec& r = recs[k];
@@ -309,7 +305,7 @@ lp_status lp_batch_create(const lp_beam_desc* beams, int count, const lp_batch_o
       }
     }
   }
-  std::vector<Item> items;
+  items.clear();
   auto emit = [&](int g, int pass) {
     for (int k = groups[g].first; k < groups[g].second; ++k) {
       const int tiles = pass == 1 ? col_tiles(recs[k].n) : row_tiles(recs[k].n);
@@ -325,6 +321,28 @@ lp_status lp_batch_create(const lp_beam_desc* beams, int count, const lp_batch_o
       if (g >= 0 && g < ng) emit(g, pass);
     }
   if (opt.debug_unsatisfiable) items.back().need += 1 << 30;
+
+  return LP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+lp_status lp_batch_create(const lp_beam_desc* beams, int count, const lp_batch_options* options,
+                          lp_batch** out) {
+  if (!out) return fail(LP_ERR_INVALID_ARGUMENT, "lp_batch_create: out is NULL");
+  *out = nullptr;
+  std::vector<BeamRec> recs;
+  std::vector<Item> items;
+  lp_batch_options opt;
+  lp_status s = plan_batch(beams, count, options, recs, items, opt);
+  if (s != LP_OK) return s;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  s = lp_init(dev);
+  if (s != LP_OK) return s;
 
   BatchPlan* p = new (std::nothrow) BatchPlan();
   if (!p) return fail(LP_ERR_OUT_OF_MEMORY, "lp_batch_create: host allocation failed");
@@ -372,6 +390,22 @@ lp_status lp_batch_create(const lp_beam_desc* beams, int count, const lp_batch_o
   b->plan = *p;
   delete p;
   *out = b;
+  return LP_OK;
+}
+
+lp_status lp_batch_plan(const lp_beam_desc* beams, int count, const lp_batch_options* options,
+                        int* n_items, long long* n_tiles, long long* n_points) {
+  std::vector<BeamRec> recs;
+  std::vector<Item> items;
+  lp_batch_options opt;
+  lp_status s = plan_batch(beams, count, options, recs, items, opt);
+  if (s != LP_OK) return s;
+  long long tiles = 0, points = 0;
+  for (const Item& it : items) tiles += it.ntiles;
+  for (const BeamRec& r : recs) points += (long long)r.n * r.n;
+  if (n_items) *n_items = (int)items.size();
+  if (n_tiles) *n_tiles = tiles;
+  if (n_points) *n_points = points;
   return LP_OK;
 }
 

@@ -3,7 +3,9 @@
 Beams are independent, so a multi-GPU batch is each rank running its own
 shard with no data-path collective.  Two gloo ranks on CPU check that every
 rank derives the same partition on its own, that the shards are disjoint and
-cover the batch, that the points are balanced, and that gathering the
+cover the batch, that the points are balanced, that each rank's shard plan
+(the library's own work-queue planner, lp_batch_plan, which makes no CUDA
+call) covers exactly its beams' tiles and points, and that gathering the
 per-rank results (oracle propagation of each shard's beams) reproduces the
 single-rank run.
 """
@@ -16,7 +18,7 @@ import torch
 import torch.distributed as dist
 import torch.multiprocessing as mp
 
-from lightprop2d_gb300.batch import partition_beams
+from lightprop2d_gb300.batch import partition_beams, plan_info, shard
 from oracle import lp_oracle as O
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -36,6 +38,9 @@ def _beam(i, n):
 
 
 SIZES = [64, 16, 32, 64, 16, 16, 32, 64, 16, 32, 16, 64, 32]
+# the uneven batch's size mix (64% 256^2, 25% 512^2, 9% 1024^2, 2% 2048^2), 100 beams
+BATCH = [256] * 64 + [512] * 25 + [1024] * 9 + [2048] * 2
+TILE_POINTS = 4096  # points per batch tile (lp_batch.cu)
 
 
 def _worker(rank, world, port, q):
@@ -44,8 +49,13 @@ def _worker(rank, world, port, q):
     try:
         parts = partition_beams(SIZES, world)
         mine = {i: _beam(i, SIZES[i]) for i in parts[rank]}
+        # this rank's shard of the uneven batch, planned by the library
+        own = shard(BATCH, world, rank)
+        sizes = [BATCH[i] for i in own]
+        plan = plan_info(sizes, 0.1, 632e-7, [0.5 + 0.01 * i for i in own],
+                         lens_f=[5.0] * len(own))
         gathered = [None] * world
-        dist.all_gather_object(gathered, (parts, mine))
+        dist.all_gather_object(gathered, (parts, mine, own, plan))
         if rank == 0:
             q.put(gathered)
         dist.barrier()
@@ -81,8 +91,21 @@ def test_two_gloo_ranks_reproduce_single_rank():
         assert p.exitcode == 0
     parts = [g[0] for g in gathered]
     assert parts[0] == parts[1]
+    # shard plans: disjoint, covering, each exactly its beams' 3 passes of tiles
+    owns = [set(g[2]) for g in gathered]
+    assert not (owns[0] & owns[1]) and sorted(owns[0] | owns[1]) == list(range(len(BATCH)))
+    total = plan_info(BATCH, 0.1, 632e-7, 1.0)
+    for own, plan in ((g[2], g[3]) for g in gathered):
+        pts = sum(BATCH[i] ** 2 for i in own)
+        assert plan["points"] == pts
+        assert plan["tiles"] == 3 * pts // TILE_POINTS
+        assert plan["items"] > 0
+    assert sum(g[3]["points"] for g in gathered) == total["points"]
+    assert sum(g[3]["tiles"] for g in gathered) == total["tiles"]
+    loads = [g[3]["points"] for g in gathered]
+    assert max(loads) - min(loads) <= max(BATCH) ** 2
     merged = {}
-    for _, mine in gathered:
+    for _, mine, _, _ in gathered:
         assert not (set(mine) & set(merged))
         merged.update(mine)
     assert sorted(merged) == list(range(len(SIZES)))
