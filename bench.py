@@ -343,8 +343,8 @@ def next_rows_section(dev, stream, hbm):
     f = torch.randn(n, n, dtype=torch.complex64, device=dev)
     out = {}
     mom = torch.empty(5, dtype=torch.float64, device=dev)
-    out["beam_moments"] = row(t_us(lambda: B.beam_moments(f, mom)), 2 * 8 * n * n,
-                              "two read passes (moments about the centroid)")
+    out["beam_moments"] = row(t_us(lambda: B.beam_moments(f, mom)), 8 * n * n,
+                              "one read pass + finish (moments about the centroid)")
     # coordinate_filter(f_gen=round_hole) folded into a propagate, vs a dense mask
     X = np.arange(-n // 2, n // 2) * (0.2 / n)
     gm = G.compact(P.round_hole, (0.05,), X.copy(), X.copy().reshape((-1, 1)), dev)

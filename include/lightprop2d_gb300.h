@@ -246,8 +246,10 @@ lp_status lp_iprofile_c128(const lp_cdouble* field, double* out, int n, void* st
  * I = |field|^2, jx = ix - n/2, jy = iy - n/2 (grid-index offsets):
  *   [0] sum I   [1] sum jx*I   [2] sum jy*I
  *   [3] sum (jx - xc)^2 I   [4] sum (jy - yc)^2 I,   xc = [1]/[0], yc = [2]/[0]
- * so Xc = dL*[1]/[0], D4sigma_x = 4*dL*sqrt([3]/[0]).  Two read-only passes
- * (the second moments about the centroid, like the reference); asynchronous. */
+ * so Xc = dL*[1]/[0], D4sigma_x = 4*dL*sqrt([3]/[0]).  One read pass (FP32
+ * run sums about each thread's own first row, moved to the grid centre in
+ * FP64) and a one-thread finish that takes the second moments about the
+ * centroid, like the reference; n even; asynchronous. */
 lp_status lp_beam_moments(const lp_cfloat* field, int n, double* moments, void* stream);
 /* Intensity loss of the differentiable design workload (no reference
  * counterpart: the inverse-design loop built on propagate, beam2d.py:462-490).

@@ -1,16 +1,20 @@
 // Intensity moments of a field for Beam2D.centroid / D4sigma /
-// centroid_intensity (beam2d.py:669-752): two read-only passes over the grid.
+// centroid_intensity (beam2d.py:669-752): one read pass over the grid and a
+// one-thread finish.
 //
-//   pass 1:  m0 = sum I,  m1 = sum jx*I,  m2 = sum jy*I
-//   pass 2:  m3 = sum (jx - xc)^2 I,  m4 = sum (jy - yc)^2 I,
-//            xc = m1/m0, yc = m2/m0 read from pass 1's result on the device
+//   out = m0 = sum I, m1 = sum jx*I, m2 = sum jy*I,
+//         m3 = sum (jx - xc)^2 I, m4 = sum (jy - yc)^2 I,  xc = m1/m0, yc = m2/m0
 //
-// with I = |field|^2 and jx = ix - n/2, jy = iy - n/2 (n even; grid-index offsets
-// from the centre; the caller scales by dL).  The second moments are taken
-// about the centroid, as the reference does, so an off-centre beam loses no
-// precision to cancellation.  Each thread accumulates in FP32 over a strided
-// share of the grid (8 loads in flight, tens of points), then warps and CTAs
-// reduce in FP64 and one atomicAdd per CTA lands in the 5-double result.
+// with I = |field|^2 and jx = ix - n/2, jy = iy - n/2 (n even; grid-index
+// offsets from the centre; the caller scales by dL).  A thread owns one
+// column and a run of contiguous rows starting at row r0, and accumulates
+// in FP32 about r0 (offsets below the run length, so the products stay
+// exact to FP32 rounding); it then converts its three sums to sums about the
+// grid centre in FP64 (sum (r-c)^2 I = S2 + 2 (r0-c) S1 + (r0-c)^2 S0), which
+// warps and CTAs add in FP64 (one atomicAdd per value per CTA).  The finish
+// turns the raw second moments into moments about the centroid in FP64, so
+// an off-centre beam keeps its precision without a second read pass (the
+// cancellation costs ~1e-16 (offset/width)^2).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -20,9 +24,7 @@
 
 namespace {
 
-// One 1024-thread CTA per SM with 16 loads in flight per thread keeps ~20 MB
-// in flight on GB300 (a 2048^2 grid in two round trips); few CTAs keep the
-// final FP64 atomics (3 per CTA onto the same 40 bytes) from contending.
+// 1024-thread CTAs, up to 16 loads in flight per thread.
 constexpr int kThreads = 1024;
 constexpr int kUnroll = 16;  // loads in flight per thread
 
@@ -32,102 +34,62 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// v[u] = f[i0 + u*stride] (0 past n2), all kUnroll loads issued before any
-// is used.
-__device__ __forceinline__ void load_block(float2 (&v)[kUnroll], const float2* __restrict__ f,
-                                           int i0, int stride, int n2) {
-  if (i0 + (kUnroll - 1) * stride < n2) {
+// One pass.  CTA (bx, by): columns bx*kThreads + tx, rows by*rows ..
+// by*rows + rows - 1 (lanes run along a row: coalesced).
+__global__ void __launch_bounds__(kThreads) moments_kernel(const float2* __restrict__ f, int n,
+                                                           int rows, double* out) {
+  asm volatile("griddepcontrol.launch_dependents;");
+  const int x = blockIdx.x * kThreads + threadIdx.x;
+  const int r0 = blockIdx.y * rows, r1 = min(n, r0 + rows);
+  float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+  if (x < n) {
+    const float2* col = f + x;
+    for (int r = r0; r < r1; r += kUnroll) {
+      float2 v[kUnroll];
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) v[u] = __ldg(f + i0 + u * stride);
-  } else {
+      for (int u = 0; u < kUnroll; ++u)
+        v[u] = r + u < r1 ? __ldg(col + (size_t)(r + u) * n) : make_float2(0.0f, 0.0f);
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) {
-      const int i = i0 + u * stride;
-      v[u] = i < n2 ? __ldg(f + i) : make_float2(0.0f, 0.0f);
+      for (int u = 0; u < kUnroll; ++u) {
+        const float I = fmaf(v[u].x, v[u].x, v[u].y * v[u].y);
+        const float d = (float)(r + u - r0);
+        s0 += I;
+        s1 = fmaf(d, I, s1);
+        s2 = fmaf(d * d, I, s2);
+      }
     }
   }
-}
-
-// Adds v[0..K) over the CTA into out[0..K) (one atomicAdd per value per CTA).
-template <int K>
-__device__ __forceinline__ void cta_add(const float (&v)[K], double* out) {
-  __shared__ double part[K][kThreads / 32];
+  const int h = n >> 1;
+  const double jx = (double)(x - h), dy = (double)(r0 - h);
+  const double S0 = s0, S1 = s1, S2 = s2;
+  const double v[5] = {S0, jx * S0, S1 + dy * S0, jx * jx * S0,
+                       S2 + 2.0 * dy * S1 + dy * dy * S0};
+  __shared__ double part[5][kThreads / 32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-  for (int k = 0; k < K; ++k) {
-    const double s = warp_sum((double)v[k]);
-    if (lane == 0) part[k][w] = s;
+  for (int k = 0; k < 5; ++k) {
+    const double t = warp_sum(v[k]);
+    if (lane == 0) part[k][w] = t;
   }
   __syncthreads();
   if (threadIdx.x < 32) {
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      double s = threadIdx.x < kThreads / 32 ? part[k][threadIdx.x] : 0.0;
-      s = warp_sum(s);
-      if (threadIdx.x == 0) atomicAdd(out + k, s);
+    for (int k = 0; k < 5; ++k) {
+      double t = threadIdx.x < kThreads / 32 ? part[k][threadIdx.x] : 0.0;
+      t = warp_sum(t);
+      if (threadIdx.x == 0) atomicAdd(out + k, t);
     }
   }
 }
 
-// The launch makes the grid stride (gridDim.x * kThreads points) a multiple
-// of n, so a thread's points all lie in one column: its jx is a constant
-// (sum jx I = jx * sum I) and jy advances by stride / n rows per step.
-__global__ void __launch_bounds__(kThreads) moments1_kernel(const float2* __restrict__ f,
-                                                            int n, double* out) {
-  // let the second pass's CTAs be scheduled as this pass's CTAs retire
-  asm volatile("griddepcontrol.launch_dependents;");
-  const int h = n >> 1;
-  const int n2 = n * n;
-  const int stride = (int)gridDim.x * kThreads;
-  const int first = (int)blockIdx.x * kThreads + (int)threadIdx.x;
-  const float jx = (float)((first % n) - h);
-  const float djy = (float)(stride / n);
-  float jy = (float)((first / n) - h);
-  float s0 = 0.0f, s2 = 0.0f;
-  for (int i0 = first; i0 < n2; i0 += kUnroll * stride) {
-    float2 v[kUnroll];
-    load_block(v, f, i0, stride, n2);
-#pragma unroll
-    for (int u = 0; u < kUnroll; ++u) {
-      const float I = fmaf(v[u].x, v[u].x, v[u].y * v[u].y);
-      s0 += I;
-      s2 = fmaf(fmaf((float)u, djy, jy), I, s2);
-    }
-    jy = fmaf((float)kUnroll, djy, jy);
-  }
-  const float s[3] = {s0, jx * s0, s2};
-  cta_add<3>(s, out);
-}
-
-__global__ void __launch_bounds__(kThreads) moments2_kernel(const float2* __restrict__ f,
-                                                            int n, double* out) {
-  const int h = n >> 1;
-  const int n2 = n * n;
-  const int stride = (int)gridDim.x * kThreads;
-  const int first = (int)blockIdx.x * kThreads + (int)threadIdx.x;
-  // launched with programmatic dependent launch: wait for pass 1's sums
+// Raw second moments about the grid centre -> about the centroid.
+__global__ void moments_finish_kernel(double* out) {
   asm volatile("griddepcontrol.wait;" ::: "memory");
   const double m0 = out[0];
-  const float xc = m0 > 0.0 ? (float)(out[1] / m0) : 0.0f;
-  const float yc = m0 > 0.0 ? (float)(out[2] / m0) : 0.0f;
-  const float dx = (float)((first % n) - h) - xc;
-  const float ddy = (float)(stride / n);
-  float dy = (float)((first / n) - h) - yc;
-  float s0 = 0.0f, s1 = 0.0f;
-  for (int i0 = first; i0 < n2; i0 += kUnroll * stride) {
-    float2 v[kUnroll];
-    load_block(v, f, i0, stride, n2);
-#pragma unroll
-    for (int u = 0; u < kUnroll; ++u) {
-      const float I = fmaf(v[u].x, v[u].x, v[u].y * v[u].y);
-      const float d = fmaf((float)u, ddy, dy);
-      s0 += I;
-      s1 = fmaf(d * d, I, s1);
-    }
-    dy = fmaf((float)kUnroll, ddy, dy);
+  if (m0 > 0.0) {
+    out[3] -= out[1] * out[1] / m0;
+    out[4] -= out[2] * out[2] / m0;
   }
-  const float s[2] = {dx * dx * s0, s1};
-  cta_add<2>(s, out + 3);
 }
 
 int g_sms_metrics = 0;
@@ -152,40 +114,31 @@ extern "C" lp_status lp_beam_moments(const lp_cfloat* field, int n, double* mome
     cudaDeviceGetAttribute(&g_sms_metrics, cudaDevAttrMultiProcessorCount, dev);
     if (g_sms_metrics <= 0) g_sms_metrics = 1;
   }
-  // grid: about one CTA per SM (fewer for small grids), a multiple of
-  // mult = n / gcd(n, 1024) so that the stride (grid * 1024 points) is a
-  // multiple of n.
-  const int n2 = n * n;
-  const int want = (n2 + kThreads * kUnroll - 1) / (kThreads * kUnroll);
-  int g = n, b = kThreads;
-  while (b) {
-    const int r = g % b;
-    g = b;
-    b = r;
-  }
-  const int mult = n / g;
-  int grid = want < g_sms_metrics ? want : g_sms_metrics;
-  grid = grid / mult * mult;
-  if (grid < mult) grid = mult;
+  // grid: column blocks of kThreads x row runs, about one CTA per SM (the
+  // five FP64 atomics per CTA all land on the same 40 bytes, so few CTAs)
+  const int cb = (n + kThreads - 1) / kThreads;
+  int rb = (g_sms_metrics + cb - 1) / cb;
+  if (rb > n) rb = n;
+  const int rows = (n + rb - 1) / rb;
+  rb = (n + rows - 1) / rows;
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e = cudaMemsetAsync(moments, 0, 5 * sizeof(double), st);
   if (e == cudaSuccess) {
-    moments1_kernel<<<grid, kThreads, 0, st>>>(reinterpret_cast<const float2*>(field), n,
-                                               moments);
+    moments_kernel<<<dim3(cb, rb), kThreads, 0, st>>>(reinterpret_cast<const float2*>(field), n,
+                                                      rows, moments);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(kThreads);
+    cfg.gridDim = dim3(1);
+    cfg.blockDim = dim3(1);
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    e = cudaLaunchKernelEx(&cfg, moments2_kernel, reinterpret_cast<const float2*>(field), n,
-                           moments);
+    e = cudaLaunchKernelEx(&cfg, moments_finish_kernel, moments);
   }
   if (e != cudaSuccess)
     return (lp_status)set_last_error(LP_ERR_CUDA, cudaGetErrorString(e));
