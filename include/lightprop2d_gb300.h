@@ -292,7 +292,7 @@ lp_status lp_coarse(const lp_cfloat* in, int n_in, lp_cfloat* out, int order, vo
  * nearest-point values outside the window -- what the reference's
  * scipy.interpolate.interp2d(kind="linear") does; in != out.  Also serves
  * Beam2D.lens_image (beam2d.py:513-537), whose sample grid is the field grid
- * scaled by -l1/l2 (dL_out may then differ in sign from dL_in).  n_out <= 4096. */
+ * scaled by -l1/l2 (dL_out may then differ in sign from dL_in).  n_out <= 8192. */
 lp_status lp_crop(const lp_cfloat* in, int n_in, int first, int n_keep, double x0, double dL_in,
                   lp_cfloat* out, int n_out, double dL_out, void* stream);
 

@@ -227,6 +227,23 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
 struct FF {
   float hi, lo;
 };
+
+// Sum of two pairs, accurate to ~2^-44 relative.
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  FF r;
+  r.hi = __fadd_rn(s, e);
+  r.lo = __fsub_rn(e, __fsub_rn(r.hi, s));
+  return r;
+}
+// a*b + c with the product exact (two_prod), then a pair sum.
+__device__ __forceinline__ FF ff_fma(float a, float b, FF c) {
+  FF p;
+  two_prod(a, b, p.hi, p.lo);
+  return ff_add(p, c);
+}
 __host__ __device__ inline FF ff_from_double(double d) {
   FF r;
   r.hi = (float)d;

@@ -342,8 +342,8 @@ __device__ __forceinline__ void load_row(float2 (&v)[16], const float2* in, int 
 }
 
 // Intensity moments of the thread's 16 points of row y (columns t + T*j),
-// reduced over the exchange group (FP32 per thread, FP64 across lanes and
-// warps) and added to out[0..5) with one atomic per value per group:
+// reduced over the exchange group (FP32 per thread and across a warp's
+// lanes, FP64 across warps) and added to out[0..5) with one atomic per value per group:
 // sum I, sum jx I, sum jy I, sum jx^2 I, sum jy^2 I (offsets from the centre).
 template <int N, int SY>
 __device__ __forceinline__ void tile_moments(const float2 (&v)[16], int y, int t, double* out) {
@@ -357,9 +357,13 @@ __device__ __forceinline__ void tile_moments(const float2 (&v)[16], int y, int t
     s1 = fmaf(jx, I, s1);
     s3 = fmaf(jx * jx, I, s3);
   });
-  const double jy = (double)(y - N / 2);
-  double m[5] = {(double)s0, (double)s1, jy * s0, (double)s3, jy * jy * s0};
-  __shared__ double red[2][5][32];  // [group][value][warp of the group]
+  // Warp sums in FP32 (the offsets are integers with squares below 2^24, so
+  // each product is exact to FP32 rounding), the group's warps in
+  // float-float, and one FP64 conversion per value for the atomic: FP64 runs
+  // at a small fraction of the FP32 rate on this part.
+  const float jy = (float)(y - N / 2);
+  float m[5] = {s0, s1, jy * s0, s3, jy * jy * s0};
+  __shared__ float red[2][5][32];  // [group][value][warp of the group]
   const int tid = group_tid<SY>(), lane = tid & 31, w = tid >> 5;
   const int grp = SY == 2 ? (int)(threadIdx.x >> 8) : 0;
 #pragma unroll
@@ -370,10 +374,10 @@ __device__ __forceinline__ void tile_moments(const float2 (&v)[16], int y, int t
   }
   group_sync<SY>();
   if (tid < 5) {
-    double a = 0.0;
+    FF a = {0.0f, 0.0f};
     const int nw = (SY == 2 ? 256 : (int)blockDim.x) >> 5;
-    for (int i = 0; i < nw; ++i) a += red[grp][tid][i];
-    atomicAdd(out + tid, a);
+    for (int i = 0; i < nw; ++i) a = ff_add(a, FF{red[grp][tid][i], 0.0f});
+    atomicAdd(out + tid, (double)a.hi + (double)a.lo);
   }
   group_sync<SY>();
 }

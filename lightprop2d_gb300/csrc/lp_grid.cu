@@ -75,6 +75,13 @@ __global__ void coarse_kernel(const float2* __restrict__ in, int n_in, float2* _
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
        i += (size_t)gridDim.x * blockDim.x) {
     const int y = (int)(i / n_out), x = (int)(i % n_out);
+    if (order == 2) {  // the common case: four independent loads
+      const float2* r0 = in + (size_t)(2 * y) * n_in + (size_t)x * 2;
+      const float2* r1 = r0 + n_in;
+      const float2 a = __ldg(r0), b = __ldg(r0 + 1), c = __ldg(r1), d = __ldg(r1 + 1);
+      out[i] = make_float2(((a.x + b.x) + (c.x + d.x)) * inv, ((a.y + b.y) + (c.y + d.y)) * inv);
+      continue;
+    }
     float2 s = make_float2(0.0f, 0.0f);
     for (int a = 0; a < order; ++a) {
       const float2* row = in + (size_t)(y * order + a) * n_in + (size_t)x * order;
@@ -120,38 +127,57 @@ __device__ __forceinline__ void axis_pos(int j, int half, float r_hi, float r_lo
   w = frac;
 }
 
-// One CTA per group of output rows: the column positions (window index and
-// weight) are computed once per CTA into shared memory, the row position
-// once per row, so a point costs four gathers and a bilinear blend.
-constexpr int kMaxOut = 4096;
+// A CTA owns a kThreads-wide column strip and a run of at most kMaxRun
+// output rows: a thread finds its column's window position once, the CTA's
+// row positions go to shared memory, and each thread blends four rows per
+// iteration (16 gathers in flight), so a point costs four gathers and a
+// bilinear blend.
+constexpr int kMaxOut = 8192;  // the largest grid the transforms take
+constexpr int kMaxRun = 64;
+constexpr int kCropRows = 4;
 
 __global__ void __launch_bounds__(kThreads) crop_kernel(const float2* __restrict__ in, int n_in,
                                                         int k0, int n_keep,
                                                         float2* __restrict__ out, int n_out,
-                                                        float r_hi, float r_lo, float o_hi,
-                                                        float o_lo) {
-  __shared__ int s_ix[kMaxOut];
-  __shared__ float s_wx[kMaxOut];
+                                                        int run, float r_hi, float r_lo,
+                                                        float o_hi, float o_lo) {
+  __shared__ int s_iy[kMaxRun];
+  __shared__ float s_wy[kMaxRun];
   const int half = n_out / 2;
-  for (int x = threadIdx.x; x < n_out; x += kThreads)
-    axis_pos(x, half, r_hi, r_lo, o_hi, o_lo, n_keep, s_ix[x], s_wx[x]);
+  const int y0 = blockIdx.y * run, y1 = min(n_out, y0 + run);
+  if ((int)threadIdx.x < y1 - y0)
+    axis_pos(y0 + threadIdx.x, half, r_hi, r_lo, o_hi, o_lo, n_keep, s_iy[threadIdx.x],
+             s_wy[threadIdx.x]);
+  const int x = blockIdx.x * kThreads + threadIdx.x;
+  const int xc = min(x, n_out - 1);
+  int ix;
+  float wx;
+  axis_pos(xc, half, r_hi, r_lo, o_hi, o_lo, n_keep, ix, wx);
+  const int ix1 = min(ix + 1, n_keep - 1);
+  const float ux = 1.0f - wx;
+  const float2* win = in + (size_t)k0 * n_in + k0;
   __syncthreads();
-  for (int y = blockIdx.x; y < n_out; y += gridDim.x) {
-    int iy;
-    float wy;
-    axis_pos(y, half, r_hi, r_lo, o_hi, o_lo, n_keep, iy, wy);
-    const int iy1 = min(iy + 1, n_keep - 1);
-    const float2* r0 = in + (size_t)(k0 + iy) * n_in + k0;
-    const float2* r1 = in + (size_t)(k0 + iy1) * n_in + k0;
-    const float uy = 1.0f - wy;
-    float2* orow = out + (size_t)y * n_out;
-    for (int x = threadIdx.x; x < n_out; x += kThreads) {
-      const int ix = s_ix[x], ix1 = min(ix + 1, n_keep - 1);
-      const float wx = s_wx[x], ux = 1.0f - wx;
-      const float2 a = __ldg(r0 + ix), b = __ldg(r0 + ix1), c = __ldg(r1 + ix),
-                   d = __ldg(r1 + ix1);
-      orow[x] = make_float2(uy * (ux * a.x + wx * b.x) + wy * (ux * c.x + wx * d.x),
-                            uy * (ux * a.y + wx * b.y) + wy * (ux * c.y + wx * d.y));
+  for (int y = y0; y < y1; y += kCropRows) {
+    float2 a[kCropRows], b[kCropRows], c[kCropRows], d[kCropRows];
+#pragma unroll
+    for (int u = 0; u < kCropRows; ++u) {
+      const int k = min(y + u, y1 - 1) - y0;
+      const int iy = s_iy[k], iy1 = min(iy + 1, n_keep - 1);
+      const float2* r0 = win + (size_t)iy * n_in;
+      const float2* r1 = win + (size_t)iy1 * n_in;
+      a[u] = __ldg(r0 + ix);
+      b[u] = __ldg(r0 + ix1);
+      c[u] = __ldg(r1 + ix);
+      d[u] = __ldg(r1 + ix1);
+    }
+#pragma unroll
+    for (int u = 0; u < kCropRows; ++u) {
+      if (x < n_out && y + u < y1) {
+        const float wy = s_wy[y + u - y0], uy = 1.0f - wy;
+        out[(size_t)(y + u) * n_out + x] =
+            make_float2(uy * (ux * a[u].x + wx * b[u].x) + wy * (ux * c[u].x + wx * d[u].x),
+                        uy * (ux * a[u].y + wx * b[u].y) + wy * (ux * c[u].y + wx * d[u].y));
+      }
     }
   }
 }
@@ -203,12 +229,19 @@ lp_status lp_crop(const lp_cfloat* in, int n_in, int first, int n_keep, double x
     return fail(LP_ERR_INVALID_ARGUMENT, "lp_crop: dL_in > 0 and finite, non-zero dL_out");
   if ((const void*)in == (const void*)out)
     return fail(LP_ERR_INVALID_ARGUMENT, "lp_crop: in and out must be different grids");
-  if (n_out > kMaxOut) return fail(LP_ERR_UNSUPPORTED_SIZE, "lp_crop: n_out <= 4096");
+  if (n_out > kMaxOut) return fail(LP_ERR_UNSUPPORTED_SIZE, "lp_crop: n_out <= 8192");
   const FF r = ff_from_double(dL_out / dL_in);
   const FF o = ff_from_double(x0 / dL_in);
-  crop_kernel<<<rows_grid(n_out, 4), kThreads, 0, (cudaStream_t)stream>>>(
+  // strips x row runs: about six CTAs per SM, runs of at most kMaxRun rows
+  const int strips = (n_out + kThreads - 1) / kThreads;
+  int runs = (rows_grid(1 << 30, 6) + strips - 1) / strips;
+  if (runs > n_out) runs = n_out;
+  int run = (n_out + runs - 1) / runs;
+  if (run > kMaxRun) run = kMaxRun;
+  runs = (n_out + run - 1) / run;
+  crop_kernel<<<dim3(strips, runs), kThreads, 0, (cudaStream_t)stream>>>(
       reinterpret_cast<const float2*>(in), n_in, first, n_keep, reinterpret_cast<float2*>(out),
-      n_out, r.hi, r.lo, o.hi, o.lo);
+      n_out, run, r.hi, r.lo, o.hi, o.lo);
   return launch_check("lp_crop");
 }
 

@@ -9,9 +9,12 @@
 // offsets from the centre; the caller scales by dL).  A thread owns one
 // column and a run of contiguous rows starting at row r0, and accumulates
 // in FP32 about r0 (offsets below the run length, so the products stay
-// exact to FP32 rounding); it then converts its three sums to sums about the
-// grid centre in FP64 (sum (r-c)^2 I = S2 + 2 (r0-c) S1 + (r0-c)^2 S0), which
-// warps and CTAs add in FP64 (one atomicAdd per value per CTA).  The finish
+// exact to FP32 rounding).  A warp adds its lanes' sums in FP32 about the
+// warp's first column (lane offsets 0..31), and lane 0 moves the warp's five
+// sums to the grid centre in float-float (sum (r-c)^2 I = S2 + 2 (r0-c) S1 +
+// (r0-c)^2 S0 with exact products, likewise in x); a CTA adds its warps'
+// pairs in float-float and adds the five sums to out in FP64 (one atomicAdd
+// per value per CTA).  The finish
 // turns the raw second moments into moments about the centroid in FP64, so
 // an off-centre beam keeps its precision without a second read pass (the
 // cancellation costs ~1e-16 (offset/width)^2).
@@ -20,13 +23,20 @@
 #include <cstdint>
 
 #include "lightprop2d_gb300.h"
+#include "lp_device.cuh"
 #include "lp_internal.h"
 
 namespace {
 
-// 1024-thread CTAs, up to 16 loads in flight per thread.
+using lp::FF;
+using lp::ff_add;
+using lp::ff_fma;
+
+// 1024-thread CTAs, two per SM (32 registers a thread), eight loads in
+// flight per thread: 128 KB of reads in flight per SM.
 constexpr int kThreads = 1024;
-constexpr int kUnroll = 16;  // loads in flight per thread
+constexpr int kUnroll = 8;
+constexpr int kCtasPerSm = 2;
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -36,8 +46,8 @@ __device__ __forceinline__ double warp_sum(double v) {
 
 // One pass.  CTA (bx, by): columns bx*kThreads + tx, rows by*rows ..
 // by*rows + rows - 1 (lanes run along a row: coalesced).
-__global__ void __launch_bounds__(kThreads) moments_kernel(const float2* __restrict__ f, int n,
-                                                           int rows, double* out) {
+__global__ void __launch_bounds__(kThreads, kCtasPerSm) moments_kernel(
+    const float2* __restrict__ f, int n, int rows, double* out) {
   asm volatile("griddepcontrol.launch_dependents;");
   const int x = blockIdx.x * kThreads + threadIdx.x;
   const int r0 = blockIdx.y * rows, r1 = min(n, r0 + rows);
@@ -45,13 +55,14 @@ __global__ void __launch_bounds__(kThreads) moments_kernel(const float2* __restr
   if (x < n) {
     const float2* col = f + x;
     for (int r = r0; r < r1; r += kUnroll) {
+      // unconditional loads (rows past the run re-read its last row, an L1
+      // hit, and count zero), so all kUnroll are in flight at once
       float2 v[kUnroll];
 #pragma unroll
-      for (int u = 0; u < kUnroll; ++u)
-        v[u] = r + u < r1 ? __ldg(col + (size_t)(r + u) * n) : make_float2(0.0f, 0.0f);
+      for (int u = 0; u < kUnroll; ++u) v[u] = __ldg(col + (size_t)min(r + u, r1 - 1) * n);
 #pragma unroll
       for (int u = 0; u < kUnroll; ++u) {
-        const float I = fmaf(v[u].x, v[u].x, v[u].y * v[u].y);
+        const float I = r + u < r1 ? fmaf(v[u].x, v[u].x, v[u].y * v[u].y) : 0.0f;
         const float d = (float)(r + u - r0);
         s0 += I;
         s1 = fmaf(d, I, s1);
@@ -59,26 +70,50 @@ __global__ void __launch_bounds__(kThreads) moments_kernel(const float2* __restr
       }
     }
   }
-  const int h = n >> 1;
-  const double jx = (double)(x - h), dy = (double)(r0 - h);
-  const double S0 = s0, S1 = s1, S2 = s2;
-  const double v[5] = {S0, jx * S0, S1 + dy * S0, jx * jx * S0,
-                       S2 + 2.0 * dy * S1 + dy * dy * S0};
-  __shared__ double part[5][kThreads / 32];
+  // Warp: FP32 sums about the warp's first column (lane offsets l = 0..31).
+  // Every term is non-negative, so each sum is accurate to FP32 rounding.
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const float l = (float)lane;
+  float t[5] = {s0, l * s0, l * l * s0, s1, s2};
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
-    const double t = warp_sum(v[k]);
-    if (lane == 0) part[k][w] = t;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t[k] += __shfl_down_sync(0xffffffffu, t[k], o);
+  }
+  // Lane 0 moves the warp's sums to the grid centre in float-float (integer
+  // offsets |X|, |Y| <= 4096, so X^2 and 2X are exact and every product is
+  // exact by two_prod): sum jx I = X A0 + AX1, sum jx^2 I = X^2 A0 + 2X AX1
+  // + AX2, likewise in y.  FP64 runs at a small fraction of the FP32 rate on
+  // this part, so it appears only in the five lanes that convert the CTA's
+  // sums for the atomics.
+  __shared__ FF part[5][kThreads / 32];
+  if (lane == 0) {
+    const int h = n >> 1;
+    const float X = (float)((int)(blockIdx.x * kThreads + threadIdx.x) - h);
+    const float Y = (float)(r0 - h);
+    part[0][w] = FF{t[0], 0.0f};
+    part[1][w] = ff_fma(X, t[0], FF{t[1], 0.0f});
+    part[2][w] = ff_fma(Y, t[0], FF{t[3], 0.0f});
+    part[3][w] = ff_fma(X * X, t[0], ff_fma(2.0f * X, t[1], FF{t[2], 0.0f}));
+    part[4][w] = ff_fma(Y * Y, t[0], ff_fma(2.0f * Y, t[3], FF{t[4], 0.0f}));
   }
   __syncthreads();
   if (threadIdx.x < 32) {
+    __shared__ FF fin[5];
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
-      double t = threadIdx.x < kThreads / 32 ? part[k][threadIdx.x] : 0.0;
-      t = warp_sum(t);
-      if (threadIdx.x == 0) atomicAdd(out + k, t);
+      FF a = threadIdx.x < kThreads / 32 ? part[k][threadIdx.x] : FF{0.0f, 0.0f};
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const FF b = {__shfl_down_sync(0xffffffffu, a.hi, o),
+                      __shfl_down_sync(0xffffffffu, a.lo, o)};
+        a = ff_add(a, b);
+      }
+      if (threadIdx.x == 0) fin[k] = a;
     }
+    __syncwarp();
+    if (threadIdx.x < 5)
+      atomicAdd(out + threadIdx.x, (double)fin[threadIdx.x].hi + (double)fin[threadIdx.x].lo);
   }
 }
 
@@ -114,10 +149,11 @@ extern "C" lp_status lp_beam_moments(const lp_cfloat* field, int n, double* mome
     cudaDeviceGetAttribute(&g_sms_metrics, cudaDevAttrMultiProcessorCount, dev);
     if (g_sms_metrics <= 0) g_sms_metrics = 1;
   }
-  // grid: column blocks of kThreads x row runs, about one CTA per SM (the
-  // five FP64 atomics per CTA all land on the same 40 bytes, so few CTAs)
+  // grid: column blocks of kThreads x row runs, one wave of kCtasPerSm CTAs
+  // per SM (the five FP64 atomics per CTA all land on the same 40 bytes, so
+  // few CTAs)
   const int cb = (n + kThreads - 1) / kThreads;
-  int rb = (g_sms_metrics + cb - 1) / cb;
+  int rb = (kCtasPerSm * g_sms_metrics + cb - 1) / cb;
   if (rb > n) rb = n;
   const int rows = (n + rb - 1) / rb;
   rb = (n + rows - 1) / rows;
