@@ -709,8 +709,10 @@ def main():
             a = B.propagate(s0, AREA, WL, z, write_spectrum=False)
             b = B.propagate(s0, AREA, WL, z, write_spectrum=False, flags=L.LP_FLAG_PHASE_FP32)
             torch.cuda.synchronize()
-            zerr[str(z)] = {"ff_phase": O.rel_l2(a.cpu().numpy(), fr),
-                            "fp32_phase": O.rel_l2(b.cpu().numpy(), fr)}
+            ah, bh = a.cpu().numpy(), b.cpu().numpy()
+            zerr[str(z)] = {"ff_phase": O.rel_l2(ah, fr), "fp32_phase": O.rel_l2(bh, fr),
+                            "ff_phase_energy_err": O.energy_err(ah, fr),
+                            "fp32_phase_energy_err": O.energy_err(bh, fr)}
         sweep = {}
         for nn in (512, 1024, 2048, 4096):
             rr = nslots(nn)
@@ -902,6 +904,39 @@ def main():
         e2e_t = float(t)
     e2e_err = O.rel_l2(houts[(ke - 1) % RE].numpy(), f_ref)
 
+    # The host link bounds a step: the same uploads and downloads without
+    # the propagate (both directions at once, as in the pipeline), and each
+    # direction alone.
+    def link_time(do_in, do_out):
+        def once(i):
+            k = i % RE
+            if do_in:
+                with torch.cuda.stream(s_in):
+                    dins[k].copy_(hin, non_blocking=True)
+            if do_out:
+                with torch.cuda.stream(s_out):
+                    houts[k].copy_(douts[k], non_blocking=True)
+        for i in range(RE):
+            once(i)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s_in)
+        s_out.wait_event(a)
+        for i in range(ke):
+            once(i)
+        s_in.wait_stream(s_out)
+        b.record(s_in)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / ke
+
+    link_both = link_time(True, True)
+    link_in, link_out = link_time(True, False), link_time(False, True)
+    link = {"ms_per_step_copies_only": round(link_both, 5),
+            "h2d_gbs": round(8 * n * n / link_in / 1e6, 1),
+            "d2h_gbs": round(8 * n * n / link_out / 1e6, 1),
+            "both_gbs_per_direction": round(8 * n * n / link_both / 1e6, 1),
+            "e2e_frac_of_link_bound": round(link_both / e2e_t, 4)}
+
     # ------------------------------------------------------ e2e: Beam2D --
     # The reference user's loop (tests/hole_diffraction.py:37-42 of the
     # reference): one Beam2D built from a host field, then per step
@@ -960,7 +995,9 @@ def main():
             "e2e": {"value": world * 1e3 / e2e_t, "unit": UNIT,
                     "h2d_bytes_per_step": 8 * n * n, "d2h_bytes_per_step": 8 * n * n,
                     "ms_per_step": round(e2e_t, 5), "rel_l2_vs_fp64_oracle": e2e_err,
-                    "note": "pinned H2D, propagate, D2H per step; three-stream pipeline"},
+                    "host_link": link,
+                    "note": "pinned H2D, propagate, D2H per step; three-stream pipeline; "
+                            "host_link: the same copies without the propagate"},
             "e2e_beam2d": beam2d_e2e,
             "clocks": clocks.summary(),
             "gpu_launches": 3 * args.steps,

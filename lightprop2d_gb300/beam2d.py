@@ -331,7 +331,15 @@ class Beam2D:
 
     # ----------------------------------------------------------- readouts --
     def _np(self, t):
-        return t.cpu().numpy() if self.numpy_output else t
+        """A numpy copy of t when numpy_output (a new array per call, as the
+        reference returns), else t.  The copy lands in page-locked memory from
+        torch's host allocator cache, so it runs at the host link's DMA rate
+        and a read-back loop reuses the blocks of the arrays it dropped."""
+        if not self.numpy_output:
+            return t
+        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+        h.copy_(t)
+        return h.numpy()
 
     @property
     def iprofile(self):

@@ -32,49 +32,62 @@ using lp::FF;
 using lp::ff_add;
 using lp::ff_fma;
 
-// 1024-thread CTAs, two per SM (32 registers a thread), eight loads in
-// flight per thread: 128 KB of reads in flight per SM.
-constexpr int kThreads = 1024;
-constexpr int kUnroll = 8;
-constexpr int kCtasPerSm = 2;
+// 512-thread CTAs, four per SM (32 registers a thread); a thread owns two
+// adjacent columns (one 16-byte load per row) and keeps four rows of loads
+// in flight: 128 KB of reads in flight per SM.
+constexpr int kThreads = 512;
+constexpr int kCols = 2 * kThreads;  // columns per CTA
+constexpr int kUnroll = 4;
+constexpr int kCtasPerSm = 4;
 
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// One pass.  CTA (bx, by): columns bx*kThreads + tx, rows by*rows ..
-// by*rows + rows - 1 (lanes run along a row: coalesced).
+// One pass.  CTA (bx, by): columns bx*kCols + 2*tx and the next one, rows
+// by*rows .. by*rows + rows - 1 (lanes run along a row: coalesced).  V4:
+// the field is 16-byte aligned (one float4 load per row and thread).
+template <bool V4>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm) moments_kernel(
     const float2* __restrict__ f, int n, int rows, double* out) {
   asm volatile("griddepcontrol.launch_dependents;");
-  const int x = blockIdx.x * kThreads + threadIdx.x;
+  const int x = blockIdx.x * kCols + 2 * threadIdx.x;  // n is even: both columns or neither
   const int r0 = blockIdx.y * rows, r1 = min(n, r0 + rows);
-  float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f;
+  // s*: both columns about row r0; b0: the second column's sum I
+  float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, b0 = 0.0f;
   if (x < n) {
     const float2* col = f + x;
     for (int r = r0; r < r1; r += kUnroll) {
       // unconditional loads (rows past the run re-read its last row, an L1
       // hit, and count zero), so all kUnroll are in flight at once
-      float2 v[kUnroll];
-#pragma unroll
-      for (int u = 0; u < kUnroll; ++u) v[u] = __ldg(col + (size_t)min(r + u, r1 - 1) * n);
+      float4 v[kUnroll];
 #pragma unroll
       for (int u = 0; u < kUnroll; ++u) {
-        const float I = r + u < r1 ? fmaf(v[u].x, v[u].x, v[u].y * v[u].y) : 0.0f;
-        const float d = (float)(r + u - r0);
+        const float2* p = col + (size_t)min(r + u, r1 - 1) * n;
+        if constexpr (V4) {
+          v[u] = __ldg(reinterpret_cast<const float4*>(p));
+        } else {
+          const float2 lo = __ldg(p), hi = __ldg(p + 1);
+          v[u] = make_float4(lo.x, lo.y, hi.x, hi.y);
+        }
+      }
+      const float d0 = (float)(r - r0);
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) {
+        const bool in = r + u < r1;
+        const float Ia = in ? fmaf(v[u].x, v[u].x, v[u].y * v[u].y) : 0.0f;
+        const float Ib = in ? fmaf(v[u].z, v[u].z, v[u].w * v[u].w) : 0.0f;
+        const float I = Ia + Ib, d = d0 + (float)u;
         s0 += I;
         s1 = fmaf(d, I, s1);
         s2 = fmaf(d * d, I, s2);
+        b0 += Ib;
       }
     }
   }
-  // Warp: FP32 sums about the warp's first column (lane offsets l = 0..31).
-  // Every term is non-negative, so each sum is accurate to FP32 rounding.
+  // Warp: FP32 sums about the warp's first column (the thread's columns sit
+  // at offsets 2l and 2l+1, l = lane: sum c I = 2l s0 + b0, sum c^2 I =
+  // 4l^2 s0 + (4l+1) b0).  Every term is non-negative, so each sum is
+  // accurate to FP32 rounding.
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const float l = (float)lane;
-  float t[5] = {s0, l * s0, l * l * s0, s1, s2};
+  const float l2 = (float)(2 * lane);
+  float t[5] = {s0, fmaf(l2, s0, b0), fmaf(l2 * l2, s0, (2.0f * l2 + 1.0f) * b0), s1, s2};
 #pragma unroll
   for (int k = 0; k < 5; ++k) {
 #pragma unroll
@@ -89,7 +102,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) moments_kernel(
   __shared__ FF part[5][kThreads / 32];
   if (lane == 0) {
     const int h = n >> 1;
-    const float X = (float)((int)(blockIdx.x * kThreads + threadIdx.x) - h);
+    const float X = (float)((int)(blockIdx.x * kCols + 2 * threadIdx.x) - h);
     const float Y = (float)(r0 - h);
     part[0][w] = FF{t[0], 0.0f};
     part[1][w] = ff_fma(X, t[0], FF{t[1], 0.0f});
@@ -149,10 +162,10 @@ extern "C" lp_status lp_beam_moments(const lp_cfloat* field, int n, double* mome
     cudaDeviceGetAttribute(&g_sms_metrics, cudaDevAttrMultiProcessorCount, dev);
     if (g_sms_metrics <= 0) g_sms_metrics = 1;
   }
-  // grid: column blocks of kThreads x row runs, one wave of kCtasPerSm CTAs
-  // per SM (the five FP64 atomics per CTA all land on the same 40 bytes, so
-  // few CTAs)
-  const int cb = (n + kThreads - 1) / kThreads;
+  // grid: column blocks of kCols x row runs, one wave of kCtasPerSm CTAs per
+  // SM (the five FP64 atomics per CTA all land on the same 40 bytes, so few
+  // CTAs)
+  const int cb = (n + kCols - 1) / kCols;
   int rb = (kCtasPerSm * g_sms_metrics + cb - 1) / cb;
   if (rb > n) rb = n;
   const int rows = (n + rb - 1) / rb;
@@ -160,8 +173,11 @@ extern "C" lp_status lp_beam_moments(const lp_cfloat* field, int n, double* mome
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e = cudaMemsetAsync(moments, 0, 5 * sizeof(double), st);
   if (e == cudaSuccess) {
-    moments_kernel<<<dim3(cb, rb), kThreads, 0, st>>>(reinterpret_cast<const float2*>(field), n,
-                                                      rows, moments);
+    const float2* f = reinterpret_cast<const float2*>(field);
+    if ((reinterpret_cast<uintptr_t>(field) & 15u) == 0)
+      moments_kernel<true><<<dim3(cb, rb), kThreads, 0, st>>>(f, n, rows, moments);
+    else
+      moments_kernel<false><<<dim3(cb, rb), kThreads, 0, st>>>(f, n, rows, moments);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
@@ -207,14 +223,19 @@ __global__ void __launch_bounds__(kLossThreads) mse_sum_kernel(const float2* __r
       s = fmaf(d, d, s);
     }
   }
-  __shared__ double part[kLossThreads / 32];
-  double a = warp_sum((double)s);
-  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = a;
+  // non-negative terms: FP32 warp sums, the CTA's warps in float-float, one
+  // FP64 conversion for the atomic (FP64 runs at a small fraction of the
+  // FP32 rate on this part)
+  __shared__ float part[kLossThreads / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
   __syncthreads();
-  if (threadIdx.x < 32) {
-    a = threadIdx.x < kLossThreads / 32 ? part[threadIdx.x] : 0.0;
-    a = warp_sum(a);
-    if (threadIdx.x == 0) atomicAdd(out, a);
+  if (threadIdx.x == 0) {
+    FF a = {0.0f, 0.0f};
+#pragma unroll
+    for (int i = 0; i < kLossThreads / 32; ++i) a = ff_add(a, FF{part[i], 0.0f});
+    atomicAdd(out, (double)a.hi + (double)a.lo);
   }
 }
 
