@@ -60,6 +60,19 @@ def test_propagate_field_c128_with_every_multiplier(n, area, z):
     assert np.linalg.norm(H(ip) - np.abs(want) ** 2) / np.linalg.norm(np.abs(want) ** 2) < TOL128
 
 
+@pytest.mark.parametrize("scale", [1e-20, 1e20])
+def test_propagate_field_c128_far_from_unit_magnitude(scale):
+    """The transforms carry float-float pairs (FP32's exponent range): fields
+    far from unit magnitude keep complex128-level agreement."""
+    from lightprop2d_gb300 import backend as B
+    n, area, z, wl = 256, 0.05, 0.7, 632 * nm
+    x = _rand(n, 7) * scale
+    g = O.grids(area, n, wl)
+    _, want = O.propagate(O.fft2(x), g["Kz"], z)
+    got = B.propagate_field(torch.as_tensor(x, device="cuda"), area, wl, z)
+    assert O.rel_l2(H(got), want) < TOL128
+
+
 def test_config2_2048_c128_against_the_reference_run(golden):
     import lightprop2d_gb300 as lp
     b = lp.Beam2D(2 * mm, 2048, 632 * nm, init_field_gen=lp.gaussian_beam,
