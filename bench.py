@@ -724,7 +724,7 @@ def main():
                               "effective_gbs": round(16 * nn * nn / (ms * 1e-3) / 1e9, 1)}
             del sl
         # complex128 (complex_bits=128, the reference's default dtype): the
-        # FP64 family on the same workload, a few steps
+        # complex128 family (float-float transforms) on the same workload
         z128_in = torch.as_tensor(O.gaussian(n, AREA, 1.0, WAIST).astype(np.complex128),
                                   device=dev)
         z128_out = torch.empty_like(z128_in)
@@ -740,7 +740,8 @@ def main():
         extra["complex128_propagate"] = {
             "ms": round(statistics.fmean(zms), 4),
             "rel_l2_vs_fp64_oracle": O.rel_l2(z128_out.cpu().numpy(), z_ref),
-            "note": "lp_propagate_field_c128: FP64 transforms, float64 transfer function"}
+            "note": "lp_propagate_field_c128: float-float transforms on the FP32 pipes, "
+                    "the reference's float64 Kz and phase"}
         del z128_in, z128_out
         st = statistics.fmean(st_ms)
         extra.update({

@@ -195,10 +195,14 @@ lp_status lp_iprofile(const lp_cfloat* field, float* out, int n, void* stream);
 
 /* ---- complex128 (complex_bits=128, the reference's default dtype,
  * beam2d.py:88, :112-113) ----
- * The same operations with complex128 grids (16-byte aligned), FP64
- * transforms and the reference's float64 transfer function and lens phase
- * (beam2d.py:305-308, :485-489, :508-510), so results agree with its numpy
- * complex128 path to round-off.  Masks: any lp_mask_type (LP_MASK_SEP_C128
+ * The same operations with complex128 grids (16-byte aligned).  Transforms
+ * run in float-float arithmetic (48 significant bits) on the FP32 pipes;
+ * the transfer function's Kz and phase and the lens phase are the
+ * reference's float64 expressions (beam2d.py:305-308, :485-489, :508-510),
+ * so results agree with its numpy complex128 path to ~1e-14 relative.
+ * Values keep that precision for magnitudes in ~[1e-30, 1e30] (FP32's
+ * exponent range, allowing for the N^2 gain of a transform); magnitudes
+ * below 2^-126 flush to zero.  Masks: any lp_mask_type (LP_MASK_SEP_C128
  * included), promoted to complex128.  Flags: LP_FLAG_EVANESCENT_MASK, and
  * LP_FLAG_SPECTRUM_READONLY for lp_propagate_c128.  npoints as for the
  * complex64 entry points.  The first call of a size on a device builds

@@ -148,7 +148,7 @@ def propagate_field(field: torch.Tensor, area_size: float, wl: float, z: float,
                     iprofile_out=None, lens_f: float = 0.0, xmask=None,
                     xmask_phase: bool = False, kmask=None, flags: int = 0) -> torch.Tensor:
     """Fused field -> field: [lens, xmask] -> fft2 -> [kmask] * H(z) -> ifft2.
-    complex128 fields run the FP64 family (iprofile_out float64)."""
+    complex128 fields run the complex128 family (iprofile_out float64)."""
     n, sfx = _zgrid(field, "field")
     out = torch.empty_like(field) if out is None else out
     _grid(out, "out", field.dtype)

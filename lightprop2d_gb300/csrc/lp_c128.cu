@@ -420,7 +420,8 @@ enum ZMode { Z_FWD = 0, Z_INV = 1, Z_FUSED = 2 };
 // [spectrum write], scale, inverse.  IN_D / OUT_D: the pass reads / writes
 // complex128 (else float-float intermediates).
 template <int N, int MODE, bool IN_D, bool OUT_D>
-__global__ void __launch_bounds__(ZGeo<N>::NT) zline_kernel(const void* __restrict__ in,
+__global__ void __launch_bounds__(ZGeo<N>::NT, ZGeo<N>::NT <= 256 ? (MODE == Z_FUSED ? 2 : 3) : 1)
+    zline_kernel(const void* __restrict__ in,
                                                            void* out, ZOps o,
                                                            const zf* __restrict__ tw) {
   using G = ZGeo<N>;
