@@ -78,7 +78,8 @@ constexpr int kMaxLog = 13;  // 8192
 
 template <int N>
 struct ZGeo {
-  static constexpr int TL = N >= 16 ? N / 16 : 1;        // threads per line
+  static constexpr int PT = 8;                            // points per thread
+  static constexpr int TL = N >= PT ? N / PT : 1;         // threads per line
   static constexpr int L = TL >= 256 ? 1 : 256 / TL;     // lines per CTA
   static constexpr int NT = TL * L;
   static constexpr int HT = N / 2 + 1;                   // H table entries per line
@@ -339,7 +340,7 @@ __device__ __forceinline__ zf zh_value(const ZOps& o, double a, int j) {
 }
 
 // In-place Stockham transform of one line (buf, N points) by TL threads
-// (t = 0..TL-1), 16 points per thread per stage.  S = -1 forward, +1 inverse
+// (t = 0..TL-1), PT points per thread per stage.  S = -1 forward, +1 inverse
 // (unscaled).  tw[k] = W_N^k.  Barriers are CTA-wide (every line of the CTA
 // runs the same stages).
 template <int N, int R, int S>
@@ -406,7 +407,7 @@ enum ZMode { Z_FWD = 0, Z_INV = 1, Z_FUSED = 2 };
 // [spectrum write], scale, inverse.  IN_D / OUT_D: the pass reads / writes
 // complex128 (else float-float intermediates).
 template <int N, int MODE, bool IN_D, bool OUT_D>
-__global__ void __launch_bounds__(ZGeo<N>::NT, ZGeo<N>::NT <= 256 ? (MODE == Z_FUSED ? 2 : 3) : 1)
+__global__ void __launch_bounds__(ZGeo<N>::NT, ZGeo<N>::NT <= 256 ? (MODE == Z_FUSED ? 3 : 4) : 1)
     zline_kernel(const void* __restrict__ in,
                                                            void* out, ZOps o,
                                                            const zf* __restrict__ tw) {
@@ -418,7 +419,7 @@ __global__ void __launch_bounds__(ZGeo<N>::NT, ZGeo<N>::NT <= 256 ? (MODE == Z_F
   const size_t base = (size_t)line * N;
   const bool live = line < N;  // N < L: a CTA has more line slots than lines
 #pragma unroll
-  for (int i = 0; i < 16 && i * G::TL < N; ++i) {
+  for (int i = 0; i < G::PT && i * G::TL < N; ++i) {
     const int x = t + G::TL * i;
     zf v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (live) {
@@ -449,7 +450,7 @@ __global__ void __launch_bounds__(ZGeo<N>::NT, ZGeo<N>::NT <= 256 ? (MODE == Z_F
     }
     __syncthreads();
 #pragma unroll
-    for (int i = 0; i < 16 && i * G::TL < N; ++i) {
+    for (int i = 0; i < G::PT && i * G::TL < N; ++i) {
       const int ky = t + G::TL * i;
       zf v = buf[ky];
       if (o.apply_h) v = zf_mul(v, hb[ky <= N / 2 ? ky : N - ky]);
@@ -462,7 +463,7 @@ __global__ void __launch_bounds__(ZGeo<N>::NT, ZGeo<N>::NT <= 256 ? (MODE == Z_F
   }
   if (!live) return;
 #pragma unroll
-  for (int i = 0; i < 16 && i * G::TL < N; ++i) {
+  for (int i = 0; i < G::PT && i * G::TL < N; ++i) {
     const int x = t + G::TL * i;
     zf v = buf[x];
     if (MODE == Z_INV) {
