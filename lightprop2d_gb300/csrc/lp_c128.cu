@@ -94,7 +94,7 @@ __global__ void zspectral_kernel(const z2* __restrict__ in, z2* out, int n, ZOps
        i += (long long)gridDim.x * blockDim.x) {
     const int ky = (int)(i / n), kx = (int)(i - (long long)ky * n);
     z2 v = in[i];
-    if (o.apply_h || o.kmask) v = zmul(v, zkmul(o, ky, kx, n));
+    if (o.apply_h || o.kmask) v = zf_to_z2(zf_mul(z2_to_zf(v), zkmul_ff(o, ky, kx, n)));
     if (o.spectrum_out) o.spectrum_out[i] = v;
     out[i] = zscale(v, o.scale);
   }
@@ -105,7 +105,7 @@ __global__ void zxmul_kernel(const z2* __restrict__ in, z2* out, int n, ZOps o) 
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
        i += (long long)gridDim.x * blockDim.x) {
     const int y = (int)(i / n), x = (int)(i - (long long)y * n);
-    out[i] = zmul(in[i], zxmul(o, y, x, n));
+    out[i] = zf_to_z2(zf_mul(z2_to_zf(in[i]), zxmul_ff(o, y, x, n)));
   }
 }
 
@@ -484,6 +484,23 @@ lp_status lp_propagate_c128(lp_cdouble* spectrum, lp_cdouble* field, int n, doub
   k.kmask = kmask_type ? kmask : nullptr;
   k.kmask_type = kmask_type;
   if (!(flags & LP_FLAG_SPECTRUM_READONLY)) k.spectrum_out = reinterpret_cast<z2*>(spectrum);
+  if (is_pow2(n)) {
+    // rows: k multipliers on load (+ spectrum write), inverse row FFT; T;
+    // inverse column FFT, 1/N^2; T
+    const zf* tw;
+    s = ztables(n, st, &tw);
+    if (s != LP_OK) return s;
+    ZOps inv = zops_none();
+    inv.scale = 1.0 / ((double)n * n);
+    cudaError_t e = zline_any(n, Z_KINV, true, false, spectrum, field, k, tw, st);
+    if (e == cudaSuccess) e = ztranspose(reinterpret_cast<z2*>(field), n, st);
+    if (e == cudaSuccess)
+      e = zline_any(n, Z_INV, false, true, field, field, inv, tw, st);
+    if (e == cudaSuccess) e = ztranspose(reinterpret_cast<z2*>(field), n, st);
+    if (e != cudaSuccess)
+      return zfail(LP_ERR_CUDA, "complex128 propagate: %s", cudaGetErrorString(e));
+    return LP_OK;
+  }
   zspectral_kernel<<<zblocks((long long)n * n), 256, 0, st>>>(
       reinterpret_cast<const z2*>(spectrum), reinterpret_cast<z2*>(field), n, k);
   cudaError_t e = cudaGetLastError();

@@ -129,43 +129,6 @@ __device__ __forceinline__ z2 zmask(const void* mask, int type, int y, int x, in
   }
 }
 
-// x-domain multiplier at (y, x): the reference's lens phase
-// (X^2+Y^2)*k0/(2f) with X = (x - (n+1)/2) dL (beam2d.py:299-300, :508-510)
-// times the mask.
-__device__ __forceinline__ z2 zxmul(const ZOps& o, int y, int x, int n) {
-  z2 m = make_double2(1.0, 0.0);
-  if (o.lens) {
-    const double X = (double)(x - (n + 1) / 2) * o.dL, Y = (double)(y - (n + 1) / 2) * o.dL;
-    double s, c;
-    sincos((X * X + Y * Y) * o.lens_c, &s, &c);
-    m = make_double2(c, s);
-  }
-  if (o.xmask) m = zmul(m, zmask(o.xmask, o.xmask_type, y, x, n));
-  return m;
-}
-
-// H at (ky, kx) as beam2d.py computes it: Kx = fftfreq(n, dL),
-// Kz = nan_to_num(sqrt(k0**2 - Kx**2 - Ky**2)), phase = 2*pi*(trunc(Kz z) - Kz z).
-__device__ __forceinline__ z2 zkmul(const ZOps& o, int ky, int kx, int n) {
-  z2 m = make_double2(1.0, 0.0);
-  if (o.apply_h) {
-    const int h = (n + 1) / 2;
-    const double fx = (double)(kx < h ? kx : kx - n) * o.val;
-    const double fy = (double)(ky < h ? ky : ky - n) * o.val;
-    const double v = (o.k0 * o.k0 - fx * fx) - fy * fy;
-    if (v >= 0.0) {
-      const double dk = sqrt(v) * o.z;
-      double s, c;
-      sincos(2.0 * kPi * (trunc(dk) - dk), &s, &c);
-      m = make_double2(c, s);
-    } else if (o.evan_mask) {
-      m = make_double2(0.0, 0.0);
-    }
-  }
-  if (o.kmask) m = zmul(m, zmask(o.kmask, o.kmask_type, ky, kx, n));
-  return m;
-}
-
 // ------------------------------------------------------ float-float values --
 // zf = (re.hi, re.lo, im.hi, im.lo), 16 bytes like a double2.
 using zf = float4;
@@ -339,6 +302,60 @@ __device__ __forceinline__ zf zh_value(const ZOps& o, double a, int j) {
   return o.evan_mask ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : make_float4(1.0f, 0.0f, 0.0f, 0.0f);
 }
 
+// 1/(2 pi) as a double-double (the pair sums to it within 6e-34).
+constexpr double kInv2PiH = 0.15915494309189535;
+constexpr double kInv2PiL = -9.839338337591243e-18;
+
+// x-domain multiplier at (y, x) as float-float: the reference's lens phase
+// (X^2+Y^2)*k0/(2f) with X = (x - (n+1)/2) dL (beam2d.py:299-300, :508-510)
+// evaluated in FP64, turned into turns by the double-double 1/(2 pi) (error
+// ~1e-16 turn for any phase below ~1e15 rad) and taken by zcis_2pi; times
+// the mask.
+__device__ __forceinline__ zf zxmul_ff(const ZOps& o, int y, int x, int n) {
+  zf m = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+  if (o.lens) {
+    const double X = (double)(x - (n + 1) / 2) * o.dL, Y = (double)(y - (n + 1) / 2) * o.dL;
+    const double ph = (X * X + Y * Y) * o.lens_c;
+    const double p = ph * kInv2PiH;
+    const double e = fma(ph, kInv2PiH, -p) + ph * kInv2PiL;
+    m = zcis_2pi((p - rint(p)) + e);
+  }
+  if (o.xmask) m = zf_mul(m, z2_to_zf(zmask(o.xmask, o.xmask_type, y, x, n)));
+  return m;
+}
+
+// k-domain multiplier at (ky, kx) as float-float: H as zh_value computes it
+// (the reference's float64 Kz and phase), times the mask.
+__device__ __forceinline__ zf zkmul_ff(const ZOps& o, int ky, int kx, int n) {
+  zf m = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+  if (o.apply_h) {
+    const int h = (n + 1) / 2;
+    const double fx = (double)(kx < h ? kx : kx - n) * o.val;
+    const double fy = (double)(ky < h ? ky : ky - n) * o.val;
+    const double v = (o.k0 * o.k0 - fx * fx) - fy * fy;
+    if (v >= 0.0) {
+      const double dk = sqrt(v) * o.z;
+      m = zcis_2pi(trunc(dk) - dk);
+    } else if (o.evan_mask) {
+      m = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+  }
+  if (o.kmask) m = zf_mul(m, z2_to_zf(zmask(o.kmask, o.kmask_type, ky, kx, n)));
+  return m;
+}
+
+// H at ky (fy2 = fy^2 of this row) and |kx| = j, in the reference's order
+// (k0^2 - Kx^2) - Ky^2.
+__device__ __forceinline__ zf zh_value_kx(const ZOps& o, double fy2, int j) {
+  const double fx = (double)j * o.val;
+  const double v = (o.k0 * o.k0 - fx * fx) - fy2;
+  if (v >= 0.0) {
+    const double dk = sqrt(v) * o.z;
+    return zcis_2pi(trunc(dk) - dk);
+  }
+  return o.evan_mask ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+}
+
 // In-place Stockham transform of one line (buf, N points) by TL threads
 // (t = 0..TL-1), PT points per thread per stage.  S = -1 forward, +1 inverse
 // (unscaled).  tw[k] = W_N^k.  Barriers are CTA-wide (every line of the CTA
@@ -399,15 +416,16 @@ __device__ __forceinline__ void zfft(zf* buf, int t, const zf* __restrict__ tw) 
   }
 }
 
-enum ZMode { Z_FWD = 0, Z_INV = 1, Z_FUSED = 2 };
+enum ZMode { Z_FWD = 0, Z_INV = 1, Z_FUSED = 2, Z_KINV = 3 };
 
 // One line pass over N lines.  Z_FWD: [pre x multiplier] forward; Z_INV:
 // inverse, scale, [post x multiplier], [iprofile]; Z_FUSED (lines are
 // columns after a transpose; line index = kx): forward, k multipliers,
-// [spectrum write], scale, inverse.  IN_D / OUT_D: the pass reads / writes
+// [spectrum write], scale, inverse; Z_KINV (lines are spectrum rows, line
+// index = ky): k multipliers, [spectrum write], inverse.  IN_D / OUT_D: the pass reads / writes
 // complex128 (else float-float intermediates).
 template <int N, int MODE, bool IN_D, bool OUT_D>
-__global__ void __launch_bounds__(ZGeo<N>::NT, ZGeo<N>::NT <= 256 ? (MODE == Z_FUSED ? 3 : 4) : 1)
+__global__ void __launch_bounds__(ZGeo<N>::NT, ZGeo<N>::NT <= 256 ? (MODE >= Z_FUSED ? 3 : 4) : 1)
     zline_kernel(const void* __restrict__ in,
                                                            void* out, ZOps o,
                                                            const zf* __restrict__ tw) {
@@ -418,23 +436,50 @@ __global__ void __launch_bounds__(ZGeo<N>::NT, ZGeo<N>::NT <= 256 ? (MODE == Z_F
   zf* buf = zs + (size_t)g * N;
   const size_t base = (size_t)line * N;
   const bool live = line < N;  // N < L: a CTA has more line slots than lines
+  if constexpr (MODE == Z_KINV) {
+    // H of this row (ky = line) at |kx| = 0..N/2 once each (H(kx, ky) =
+    // H(-kx, ky)), filled while the row's loads are in flight
+    zf v[G::PT];
 #pragma unroll
-  for (int i = 0; i < G::PT && i * G::TL < N; ++i) {
-    const int x = t + G::TL * i;
-    zf v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (live) {
-      if constexpr (IN_D) {
-        v = z2_to_zf(reinterpret_cast<const z2*>(in)[base + x]);
-      } else {
-        v = reinterpret_cast<const zf*>(in)[base + x];
-      }
+    for (int i = 0; i < G::PT && i * G::TL < N; ++i)
+      v[i] = live ? z2_to_zf(reinterpret_cast<const z2*>(in)[base + t + G::TL * i])
+                  : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    zf* hb = zs + (size_t)G::L * N + (size_t)g * G::HT;
+    if (o.apply_h) {
+      const int h = (N + 1) / 2;
+      const double fy = (double)(line < h ? line : line - N) * o.val;
+      const double fy2 = fy * fy;
+      for (int j = t; j < G::HT; j += G::TL) hb[j] = zh_value_kx(o, fy2, j);
     }
-    if (MODE == Z_FWD && live && (o.lens || o.xmask) && !o.post)
-      v = zf_mul(v, z2_to_zf(zxmul(o, line, x, N)));
-    buf[x] = v;
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < G::PT && i * G::TL < N; ++i) {
+      const int kx = t + G::TL * i;
+      zf w = v[i];
+      if (o.apply_h) w = zf_mul(w, hb[kx <= N / 2 ? kx : N - kx]);
+      if (o.kmask && live) w = zf_mul(w, z2_to_zf(zmask(o.kmask, o.kmask_type, line, kx, N)));
+      if (o.spectrum_out && live) o.spectrum_out[base + kx] = zf_to_z2(w);
+      buf[kx] = w;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < G::PT && i * G::TL < N; ++i) {
+      const int x = t + G::TL * i;
+      zf v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (live) {
+        if constexpr (IN_D) {
+          v = z2_to_zf(reinterpret_cast<const z2*>(in)[base + x]);
+        } else {
+          v = reinterpret_cast<const zf*>(in)[base + x];
+        }
+      }
+      if (MODE == Z_FWD && live && (o.lens || o.xmask) && !o.post)
+        v = zf_mul(v, zxmul_ff(o, line, x, N));
+      buf[x] = v;
+    }
   }
   __syncthreads();
-  if constexpr (MODE == Z_INV) {
+  if constexpr (MODE == Z_INV || MODE == Z_KINV) {
     zfft<N, 1>(buf, t, tw);
   } else {
     zfft<N, -1>(buf, t, tw);
@@ -468,7 +513,7 @@ __global__ void __launch_bounds__(ZGeo<N>::NT, ZGeo<N>::NT <= 256 ? (MODE == Z_F
     zf v = buf[x];
     if (MODE == Z_INV) {
       v = zf_scale(v, o.scale_h, o.scale_l);
-      if ((o.lens || o.xmask) && o.post) v = zf_mul(v, z2_to_zf(zxmul(o, line, x, N)));
+      if ((o.lens || o.xmask) && o.post) v = zf_mul(v, zxmul_ff(o, line, x, N));
       if (o.iprofile) {
         float ah, al, bh, bl, ph, pl;
         ff_mul2(v.x, v.y, v.x, v.y, ah, al);
@@ -488,7 +533,7 @@ __global__ void __launch_bounds__(ZGeo<N>::NT, ZGeo<N>::NT <= 256 ? (MODE == Z_F
 // The line-pass variants a size uses: (mode, reads complex128, writes complex128).
 #define LP_ZLINE_VARIANTS(X) \
   X(Z_FWD, true, false) X(Z_FWD, false, true) X(Z_INV, true, false) X(Z_INV, false, true) \
-  X(Z_FUSED, false, false)
+  X(Z_FUSED, false, false) X(Z_KINV, true, false)
 
 template <int N>
 cudaError_t set_smem() {
@@ -497,7 +542,7 @@ cudaError_t set_smem() {
   if (e == cudaSuccess)                                                                   \
     e = cudaFuncSetAttribute(zline_kernel<N, M, I, O>,                                    \
                              cudaFuncAttributeMaxDynamicSharedMemorySize,                 \
-                             (int)(M == Z_FUSED ? ZGeo<N>::SMEM_FUSED : ZGeo<N>::SMEM));
+                             (int)(M >= Z_FUSED ? ZGeo<N>::SMEM_FUSED : ZGeo<N>::SMEM));
   LP_ZLINE_VARIANTS(LP_ZSET)
 #undef LP_ZSET
   return e;
@@ -515,7 +560,7 @@ cudaError_t zline(int mode, bool in_d, bool out_d, const void* in, void* out, ZO
 #define LP_ZLAUNCH(M, I, O)                                                                 \
   if (!done && mode == M && in_d == I && out_d == O) {                                      \
     zline_kernel<N, M, I, O>                                                                \
-        <<<grid, G::NT, M == Z_FUSED ? G::SMEM_FUSED : G::SMEM, st>>>(in, out, o, tw);      \
+        <<<grid, G::NT, M >= Z_FUSED ? G::SMEM_FUSED : G::SMEM, st>>>(in, out, o, tw);      \
     done = true;                                                                            \
   }
   LP_ZLINE_VARIANTS(LP_ZLAUNCH)

@@ -60,6 +60,30 @@ def test_propagate_field_c128_with_every_multiplier(n, area, z):
     assert np.linalg.norm(H(ip) - np.abs(want) ** 2) / np.linalg.norm(np.abs(want) ** 2) < TOL128
 
 
+@pytest.mark.parametrize("n,area,z", [(256, 0.02, 0.9), (100, 0.01, 0.3), (2048, 0.2, 5.0)])
+def test_propagate_c128_spectrum_state(n, area, z):
+    """lp_propagate_c128 (Beam2D.propagate on the stored spectrum): H and a
+    k-domain mask applied as the inverse transform loads the rows, the
+    multiplied spectrum written back, against the oracle's complex128
+    sequence (beam2d.py:481-490); also with the spectrum left unchanged."""
+    from lightprop2d_gb300 import backend as B
+    wl = 632 * nm
+    x = _rand(n, 3 * n)
+    g = O.grids(area, n, wl)
+    km = np.exp(2j * np.pi * np.random.default_rng(2).uniform(size=(n, n)))
+    spec = O.fft2(x)
+    spec_z, want = O.propagate(spec * km, g["Kz"], z)
+    t = torch.as_tensor(spec, device="cuda")
+    f = B.propagate(t, area, wl, z, kmask=torch.as_tensor(km, device="cuda"))
+    assert O.rel_l2(H(f), want) < TOL128
+    assert O.rel_l2(H(t), spec_z) < TOL128
+    t2 = torch.as_tensor(spec, device="cuda")
+    _, want2 = O.propagate(spec, g["Kz"], z)
+    f2 = B.propagate(t2, area, wl, z, write_spectrum=False)
+    assert O.rel_l2(H(f2), want2) < TOL128
+    assert np.array_equal(H(t2), spec)
+
+
 @pytest.mark.parametrize("scale", [1e-20, 1e20])
 def test_propagate_field_c128_far_from_unit_magnitude(scale):
     """The transforms carry float-float pairs (FP32's exponent range): fields
