@@ -965,6 +965,29 @@ def main():
         o = O.OracleBeam(AREA, n, WL, init_field=O.gaussian(n, AREA, 1.0, WAIST))
         o.propagate(Z * (kb + 3))
         ip_ref = np.abs(o.field) ** 2
+        # the same loop with Beam2D's default complex_bits=128 (the dtype the
+        # reference's own scripts run in): float-float transforms, float64
+        # iprofile (32 MiB read back per step)
+        bz = Beam2D(AREA, n, WL, init_field=O.gaussian(n, AREA, 1.0, WAIST))
+        kz = max(5, min(40, args.steps))
+        with clocks.window():
+            for _ in range(2):
+                bz.propagate(Z)
+                _ = bz.iprofile
+            t0 = time.perf_counter()
+            for _ in range(kz):
+                bz.propagate(Z)
+                ipz = bz.iprofile
+            t_z = (time.perf_counter() - t0) / kz
+        oz = O.OracleBeam(AREA, n, WL, init_field=O.gaussian(n, AREA, 1.0, WAIST))
+        oz.propagate(Z * (kz + 2))
+        ipz_ref = np.abs(oz.field) ** 2
+        beam2d_c128 = {
+            "value": 1.0 / t_z, "unit": UNIT, "ms_per_step": round(t_z * 1e3, 4),
+            "d2h_bytes_per_step": 8 * n * n, "dtype": "c128 (float-float transforms)",
+            "iprofile_rel_l2_vs_fp64_oracle": float(np.linalg.norm(ipz - ipz_ref) /
+                                                    np.linalg.norm(ipz_ref)),
+            "note": "the e2e_beam2d loop with complex_bits=128 (Beam2D's default)"}
         beam2d_e2e = {
             "value": 1.0 / t_b2d, "unit": UNIT, "ms_per_step": round(t_b2d * 1e3, 4),
             "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 4 * n * n,
@@ -972,7 +995,8 @@ def main():
             "iprofile_rel_l2_vs_fp64_oracle": float(np.linalg.norm(ip - ip_ref) /
                                                     np.linalg.norm(ip_ref)),
             "note": "Beam2D(init_field=host array), then per step propagate(1 cm) and "
-                    "iprofile to numpy (the reference user's loop); host wall clock"}
+                    "iprofile to numpy (the reference user's loop); host wall clock",
+            "complex_bits_128": beam2d_c128}
     clocks.stop()
 
     if rank == 0:
