@@ -461,7 +461,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--quick", action="store_true", help="skip the sweep")
-    ap.add_argument("--only", choices=["batch", "next_rows", "propagate"],
+    ap.add_argument("--only", choices=["batch", "next_rows", "propagate", "c128"],
                     help="run one section once and print its JSON (profiling cases)")
     ap.add_argument("--n", type=int, default=2048,
                     help="grid size of --only propagate (fused propagates back to back)")
@@ -614,6 +614,26 @@ def main():
                    "effective_gbs": round(16 * nn * nn / (ms * 1e-3) / 1e9, 1),
                    "passes_ms": [round(statistics.fmean(p), 5) for p in pm],
                    "slots": rr}
+        elif args.only == "c128":
+            # complex128 fused propagates back to back (--n grid), and the
+            # spectrum-state propagate of Beam2D
+            nn = args.n
+            zi = torch.as_tensor(O.gaussian(nn, AREA, 1.0, WAIST).astype(np.complex128),
+                                 device=dev)
+            zo = torch.empty_like(zi)
+            zs = torch.fft.fft2(zi)
+            zf = torch.empty_like(zi)
+            def fused128(i):
+                B.propagate_field(zi, AREA, WL, Z, out=zo)
+                return 0
+
+            def state128(i):
+                B.propagate(zs, AREA, WL, Z, field_out=zf, write_spectrum=False)
+                return 0
+            fm, _ = timed(fused128, args.steps, args.warmup)
+            sm, _ = timed(state128, args.steps, args.warmup)
+            res = {"n": nn, "fused_ms": round(statistics.fmean(fm), 5),
+                   "spectrum_state_ms": round(statistics.fmean(sm), 5)}
         else:
             res = next_rows_section(dev, stream, peaks()[0])
         print(json.dumps({"section": args.only, **res}))
