@@ -251,18 +251,18 @@ __device__ __forceinline__ void zhorner(float sh, float sl, int sign, float ch, 
   ff_add2(sign * ch, sign * cl, ph, pl, ah, al);
 }
 
-// cos(2 pi f) + i sin(2 pi f) for a double f with |f| < 2^21, as float-float.
-// Quarter turns: 4f = q + rho (q an integer, |rho| <= 1/2, both exact), so
-// theta = rho pi/2 has |theta| <= pi/4; sin(theta)/theta and cos(theta) are
-// their Taylor series in s = theta^2 (terms from s^5 on, below 3e-8 of the
-// result, in FP32; the first five in float-float; truncation below 1e-17),
-// and the quadrant q mod 4 rotates the result.
+// cos(2 pi f) + i sin(2 pi f) for a double f with |f| < 2^50, as float-float.
+// Quarter turns in FP64: 4f = q + rho (q an integer, |rho| <= 1/2, both
+// exact), so theta = rho pi/2 has |theta| <= pi/4 and rho converts to
+// float-float within 2^-48; sin(theta)/theta and cos(theta) are their Taylor
+// series in s = theta^2 (terms from s^5 on, below 3e-8 of the result, in
+// FP32; the first five in float-float; truncation below 1e-17), and the
+// quadrant q mod 4 rotates the result.
 __device__ __forceinline__ zf zcis_2pi(double f) {
-  float fh, fl;
-  d2ff(f, fh, fl);
-  const float q = rintf(4.0f * fh);
+  const double f4 = 4.0 * f, qd = rint(f4);
   float rh, rl, th, tl, sh, sl;
-  two_sum(__fsub_rn(4.0f * fh, q), 4.0f * fl, rh, rl);
+  d2ff(f4 - qd, rh, rl);
+  const long long q = (long long)qd;
   ff_mul2(rh, rl, kHalfPiH, kHalfPiL, th, tl);
   ff_mul2(th, tl, th, tl, sh, sl);
   // FP32 tails: sin: -1/11! + s/13! - s^2/15! + s^3/17!; cos: -1/10! + ... - s^4/18!
