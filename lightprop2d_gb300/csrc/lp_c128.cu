@@ -235,13 +235,13 @@ lp_status ztables(int n, cudaStream_t st, const zf** tw) {
 
 }  // namespace
 
-cudaError_t zline_any(int n, int mode, bool in_d, bool out_d, const void* in, void* out,
-                      const ZOps& o, const float4* tw, cudaStream_t st) {
-  if (n <= 128) return zline_g16_128(n, mode, in_d, out_d, in, out, o, tw, st);
-  if (n <= 512) return zline_g256_512(n, mode, in_d, out_d, in, out, o, tw, st);
-  if (n <= 2048) return zline_g1024_2048(n, mode, in_d, out_d, in, out, o, tw, st);
-  if (n == 4096) return zline_g4096(n, mode, in_d, out_d, in, out, o, tw, st);
-  return zline_g8192(n, mode, in_d, out_d, in, out, o, tw, st);
+cudaError_t zline_any(int n, int mode, bool in_d, bool out_d, bool cols, const void* in,
+                      void* out, const ZOps& o, const float4* tw, cudaStream_t st) {
+  if (n <= 128) return zline_g16_128(n, mode, in_d, out_d, cols, in, out, o, tw, st);
+  if (n <= 512) return zline_g256_512(n, mode, in_d, out_d, cols, in, out, o, tw, st);
+  if (n <= 2048) return zline_g1024_2048(n, mode, in_d, out_d, cols, in, out, o, tw, st);
+  if (n == 4096) return zline_g4096(n, mode, in_d, out_d, cols, in, out, o, tw, st);
+  return zline_g8192(n, mode, in_d, out_d, cols, in, out, o, tw, st);
 }
 
 cudaError_t zline_smem(int n) {
@@ -266,19 +266,25 @@ ZOps zops_none() {
   return o;
 }
 
+// Columns as lines: n <= 4096 reads them in place (two adjacent columns per
+// CTA); 8192 transposes and runs row passes.
+bool zcols(int n) { return n <= 4096; }
+
 // Power-of-two n: out = [post] F^-1 [k] F [pre] in, as selected by the ops.
-//   rows (pre x ops, forward), T, lines (forward, k ops, scale, inverse), T,
-//   rows (inverse, post x ops, iprofile).
+//   rows (pre x ops, forward), columns (forward, k ops, scale, inverse),
+//   rows (inverse, post x ops, iprofile); 8192 transposes around a row pass
+//   in place of the column pass.
 lp_status zpropagate_pow2(const z2* in, z2* out, int n, const ZOps& x_pre, const ZOps& k,
                           const ZOps& x_post, cudaStream_t st) {
   const zf* tw;
   lp_status s = ztables(n, st, &tw);
   if (s != LP_OK) return s;
-  cudaError_t e = zline_any(n, Z_FWD, true, false, in, out, x_pre, tw, st);
-  if (e == cudaSuccess) e = ztranspose(out, n, st);
-  if (e == cudaSuccess) e = zline_any(n, Z_FUSED, false, false, out, out, k, tw, st);
-  if (e == cudaSuccess) e = ztranspose(out, n, st);
-  if (e == cudaSuccess) e = zline_any(n, Z_INV, false, true, out, out, x_post, tw, st);
+  const bool cols = zcols(n);
+  cudaError_t e = zline_any(n, Z_FWD, true, false, false, in, out, x_pre, tw, st);
+  if (e == cudaSuccess && !cols) e = ztranspose(out, n, st);
+  if (e == cudaSuccess) e = zline_any(n, Z_FUSED, false, false, cols, out, out, k, tw, st);
+  if (e == cudaSuccess && !cols) e = ztranspose(out, n, st);
+  if (e == cudaSuccess) e = zline_any(n, Z_INV, false, true, false, out, out, x_post, tw, st);
   if (e != cudaSuccess) return zfail(LP_ERR_CUDA, "complex128 passes: %s", cudaGetErrorString(e));
   return LP_OK;
 }
@@ -292,10 +298,11 @@ lp_status zfft2_pow2(const z2* in, z2* out, int n, int inverse, double scale, cu
   o.scale = scale;
   const int mode = inverse ? Z_INV : Z_FWD;
   ZOps first = zops_none();
-  cudaError_t e = zline_any(n, mode, true, false, in, out, first, tw, st);
-  if (e == cudaSuccess) e = ztranspose(out, n, st);
-  if (e == cudaSuccess) e = zline_any(n, mode, false, true, out, out, o, tw, st);
-  if (e == cudaSuccess) e = ztranspose(out, n, st);
+  const bool cols = zcols(n);
+  cudaError_t e = zline_any(n, mode, true, false, false, in, out, first, tw, st);
+  if (e == cudaSuccess && !cols) e = ztranspose(out, n, st);
+  if (e == cudaSuccess) e = zline_any(n, mode, false, true, cols, out, out, o, tw, st);
+  if (e == cudaSuccess && !cols) e = ztranspose(out, n, st);
   if (e != cudaSuccess) return zfail(LP_ERR_CUDA, "complex128 transform: %s", cudaGetErrorString(e));
   return LP_OK;
 }
@@ -485,18 +492,19 @@ lp_status lp_propagate_c128(lp_cdouble* spectrum, lp_cdouble* field, int n, doub
   k.kmask_type = kmask_type;
   if (!(flags & LP_FLAG_SPECTRUM_READONLY)) k.spectrum_out = reinterpret_cast<z2*>(spectrum);
   if (is_pow2(n)) {
-    // rows: k multipliers on load (+ spectrum write), inverse row FFT; T;
-    // inverse column FFT, 1/N^2; T
+    // rows: k multipliers on load (+ spectrum write), inverse row FFT;
+    // columns: inverse FFT, 1/N^2 (8192: T, rows, T)
     const zf* tw;
     s = ztables(n, st, &tw);
     if (s != LP_OK) return s;
     ZOps inv = zops_none();
     inv.scale = 1.0 / ((double)n * n);
-    cudaError_t e = zline_any(n, Z_KINV, true, false, spectrum, field, k, tw, st);
-    if (e == cudaSuccess) e = ztranspose(reinterpret_cast<z2*>(field), n, st);
-    if (e == cudaSuccess)
-      e = zline_any(n, Z_INV, false, true, field, field, inv, tw, st);
-    if (e == cudaSuccess) e = ztranspose(reinterpret_cast<z2*>(field), n, st);
+    const bool cols = zcols(n);
+    z2* fz = reinterpret_cast<z2*>(field);
+    cudaError_t e = zline_any(n, Z_KINV, true, false, false, spectrum, field, k, tw, st);
+    if (e == cudaSuccess && !cols) e = ztranspose(fz, n, st);
+    if (e == cudaSuccess) e = zline_any(n, Z_INV, false, true, cols, field, field, inv, tw, st);
+    if (e == cudaSuccess && !cols) e = ztranspose(fz, n, st);
     if (e != cudaSuccess)
       return zfail(LP_ERR_CUDA, "complex128 propagate: %s", cudaGetErrorString(e));
     return LP_OK;

@@ -41,23 +41,24 @@ struct ZOps {
 };
 
 // Line pass over the N lines of an N x N grid (n a power of two 16..8192):
-// mode Z_FWD / Z_INV / Z_FUSED; in_d / out_d: the pass reads / writes
-// complex128 (else float-float intermediates).  Defined per size group in
+// mode Z_FWD / Z_INV / Z_FUSED / Z_KINV; in_d / out_d: the pass reads /
+// writes complex128 (else float-float intermediates); cols: the lines are
+// the grid's columns (n <= 4096), else its rows.  Defined per size group in
 // lp_c128_lines_*.cu.
-cudaError_t zline_any(int n, int mode, bool in_d, bool out_d, const void* in, void* out,
-                      const ZOps& o, const float4* tw, cudaStream_t st);
+cudaError_t zline_any(int n, int mode, bool in_d, bool out_d, bool cols, const void* in,
+                      void* out, const ZOps& o, const float4* tw, cudaStream_t st);
 // Sets the line kernels' shared-memory limits for size n.
 cudaError_t zline_smem(int n);
-cudaError_t zline_g16_128(int n, int mode, bool in_d, bool out_d, const void* in, void* out,
-                          const ZOps& o, const float4* tw, cudaStream_t st);
-cudaError_t zline_g256_512(int n, int mode, bool in_d, bool out_d, const void* in, void* out,
-                           const ZOps& o, const float4* tw, cudaStream_t st);
-cudaError_t zline_g1024_2048(int n, int mode, bool in_d, bool out_d, const void* in, void* out,
-                             const ZOps& o, const float4* tw, cudaStream_t st);
-cudaError_t zline_g4096(int n, int mode, bool in_d, bool out_d, const void* in, void* out,
-                        const ZOps& o, const float4* tw, cudaStream_t st);
-cudaError_t zline_g8192(int n, int mode, bool in_d, bool out_d, const void* in, void* out,
-                        const ZOps& o, const float4* tw, cudaStream_t st);
+cudaError_t zline_g16_128(int n, int mode, bool in_d, bool out_d, bool cols, const void* in,
+                          void* out, const ZOps& o, const float4* tw, cudaStream_t st);
+cudaError_t zline_g256_512(int n, int mode, bool in_d, bool out_d, bool cols, const void* in,
+                          void* out, const ZOps& o, const float4* tw, cudaStream_t st);
+cudaError_t zline_g1024_2048(int n, int mode, bool in_d, bool out_d, bool cols, const void* in,
+                          void* out, const ZOps& o, const float4* tw, cudaStream_t st);
+cudaError_t zline_g4096(int n, int mode, bool in_d, bool out_d, bool cols, const void* in,
+                          void* out, const ZOps& o, const float4* tw, cudaStream_t st);
+cudaError_t zline_g8192(int n, int mode, bool in_d, bool out_d, bool cols, const void* in,
+                          void* out, const ZOps& o, const float4* tw, cudaStream_t st);
 cudaError_t zsmem_g16_128(int n);
 cudaError_t zsmem_g256_512(int n);
 cudaError_t zsmem_g1024_2048(int n);
@@ -76,11 +77,14 @@ __device__ __forceinline__ z2 zscale(z2 a, double s) { return make_double2(a.x *
 
 constexpr int kMaxLog = 13;  // 8192
 
-template <int N>
+// Line geometry; LMIN: least lines per CTA (2 for column passes, so that a
+// warp's loads cover whole 32-byte sectors of two adjacent columns).
+template <int N, int LMIN = 1>
 struct ZGeo {
   static constexpr int PT = 8;                            // points per thread
   static constexpr int TL = N >= PT ? N / PT : 1;         // threads per line
-  static constexpr int L = TL >= 256 ? 1 : 256 / TL;     // lines per CTA
+  static constexpr int L0 = TL >= 256 ? 1 : 256 / TL;
+  static constexpr int L = L0 < LMIN ? LMIN : L0;         // lines per CTA
   static constexpr int NT = TL * L;
   static constexpr int HT = N / 2 + 1;                   // H table entries per line
   static constexpr size_t SMEM = 16 * (size_t)L * N;
@@ -357,17 +361,18 @@ __device__ __forceinline__ zf zh_value_kx(const ZOps& o, double fy2, int j) {
 }
 
 // In-place Stockham transform of one line (buf, N points) by TL threads
-// (t = 0..TL-1), PT points per thread per stage.  S = -1 forward, +1 inverse
+// (t = 0..TL-1), PT points per thread per stage; element i of the line at
+// buf[i * LS].  S = -1 forward, +1 inverse
 // (unscaled).  tw[k] = W_N^k.  Barriers are CTA-wide (every line of the CTA
 // runs the same stages).
-template <int N, int R, int S>
+template <int N, int R, int S, int LS>
 __device__ __forceinline__ void zstage(zf* buf, int t, int ns, const zf* __restrict__ tw) {
   constexpr int TL = ZGeo<N>::TL, NB = N / R, QB = NB / TL;  // butterflies per thread
   zf v[QB * R];
 #pragma unroll
   for (int q = 0; q < QB; ++q)
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[q * R + r] = buf[t + q * TL + r * NB];
+    for (int r = 0; r < R; ++r) v[q * R + r] = buf[(t + q * TL + r * NB) * LS];
   __syncthreads();
 #pragma unroll
   for (int q = 0; q < QB; ++q) {
@@ -384,34 +389,34 @@ __device__ __forceinline__ void zstage(zf* buf, int t, int ns, const zf* __restr
     }
     const int o = (b - k) * R + k;
     if constexpr (R == 2) {
-      buf[o] = zf_add(a[0], a[1]);
-      buf[o + ns] = zf_sub(a[0], a[1]);
+      buf[o * LS] = zf_add(a[0], a[1]);
+      buf[(o + ns) * LS] = zf_sub(a[0], a[1]);
     } else {
       const zf t0 = zf_add(a[0], a[2]), t1 = zf_sub(a[0], a[2]);
       const zf t2 = zf_add(a[1], a[3]);
       zf t3 = zf_sub(a[1], a[3]);
       t3 = S < 0 ? make_float4(t3.z, t3.w, -t3.x, -t3.y)
                  : make_float4(-t3.z, -t3.w, t3.x, t3.y);  // * (S*i)
-      buf[o] = zf_add(t0, t2);
-      buf[o + ns] = zf_add(t1, t3);
-      buf[o + 2 * ns] = zf_sub(t0, t2);
-      buf[o + 3 * ns] = zf_sub(t1, t3);
+      buf[o * LS] = zf_add(t0, t2);
+      buf[(o + ns) * LS] = zf_add(t1, t3);
+      buf[(o + 2 * ns) * LS] = zf_sub(t0, t2);
+      buf[(o + 3 * ns) * LS] = zf_sub(t1, t3);
     }
   }
   __syncthreads();
 }
 
-template <int N, int S>
+template <int N, int S, int LS>
 __device__ __forceinline__ void zfft(zf* buf, int t, const zf* __restrict__ tw) {
   constexpr int LOG = ZGeo<N>::LOG;
   int ns = 1;
   if constexpr (LOG & 1) {
-    zstage<N, 2, S>(buf, t, ns, tw);
+    zstage<N, 2, S, LS>(buf, t, ns, tw);
     ns = 2;
   }
 #pragma unroll 1
   for (int s = 0; s < LOG / 2; ++s) {
-    zstage<N, 4, S>(buf, t, ns, tw);
+    zstage<N, 4, S, LS>(buf, t, ns, tw);
     ns *= 4;
   }
 }
@@ -424,17 +429,40 @@ enum ZMode { Z_FWD = 0, Z_INV = 1, Z_FUSED = 2, Z_KINV = 3 };
 // [spectrum write], scale, inverse; Z_KINV (lines are spectrum rows, line
 // index = ky): k multipliers, [spectrum write], inverse.  IN_D / OUT_D: the pass reads / writes
 // complex128 (else float-float intermediates).
-template <int N, int MODE, bool IN_D, bool OUT_D>
-__global__ void __launch_bounds__(ZGeo<N>::NT, ZGeo<N>::NT <= 256 ? (MODE >= Z_FUSED ? 3 : 4) : 1)
-    zline_kernel(const void* __restrict__ in,
-                                                           void* out, ZOps o,
-                                                           const zf* __restrict__ tw) {
-  using G = ZGeo<N>;
+// Lines per CTA of a pass: column passes take at least two adjacent columns.
+template <int N, bool COLS>
+using ZG = ZGeo<N, COLS ? 2 : 1>;
+
+template <int N, int MODE, bool COLS>
+constexpr int zmin_blocks() {
+  constexpr int nt = ZG<N, COLS>::NT;
+  return nt <= 256 ? (MODE >= Z_FUSED ? 3 : 4) : (nt <= 512 ? 2 : 1);
+}
+
+// One line pass over N lines.  Rows (COLS false): line = row, element x at
+// [line * N + x].  Columns (COLS true): line = column, element x at
+// [x * N + line]; neighbouring threads take neighbouring columns of a row
+// and the shared-memory lines interleave (element i of line g at i * L + g),
+// so loads, stores and the stage exchanges stay coalesced and conflict-free.
+// Modes: Z_FWD: [pre x multiplier] forward; Z_INV: inverse, scale, [post x
+// multiplier], [iprofile]; Z_FUSED (line index = kx): forward, k
+// multipliers, [spectrum write], scale, inverse; Z_KINV (rows of a spectrum,
+// line index = ky): k multipliers, [spectrum write], inverse.  IN_D / OUT_D:
+// the pass reads / writes complex128 (else float-float intermediates).
+template <int N, int MODE, bool IN_D, bool OUT_D, bool COLS>
+__global__ void __launch_bounds__(ZG<N, COLS>::NT, zmin_blocks<N, MODE, COLS>())
+    zline_kernel(const void* __restrict__ in, void* out, ZOps o, const zf* __restrict__ tw) {
+  using G = ZG<N, COLS>;
+  constexpr int LS = COLS ? G::L : 1;  // element stride of a line in shared memory
   extern __shared__ float4 zs[];
-  const int g = threadIdx.x / G::TL, t = threadIdx.x % G::TL;
+  const int g = COLS ? (int)(threadIdx.x % G::L) : (int)(threadIdx.x / G::TL);
+  const int t = COLS ? (int)(threadIdx.x / G::L) : (int)(threadIdx.x % G::TL);
   const int line = blockIdx.x * G::L + g;
-  zf* buf = zs + (size_t)g * N;
-  const size_t base = (size_t)line * N;
+  zf* buf = COLS ? zs + g : zs + (size_t)g * N;
+  // grid offset of element x of this line
+  auto at = [&](int x) -> size_t {
+    return COLS ? (size_t)x * N + line : (size_t)line * N + x;
+  };
   const bool live = line < N;  // N < L: a CTA has more line slots than lines
   if constexpr (MODE == Z_KINV) {
     // H of this row (ky = line) at |kx| = 0..N/2 once each (H(kx, ky) =
@@ -442,7 +470,7 @@ __global__ void __launch_bounds__(ZGeo<N>::NT, ZGeo<N>::NT <= 256 ? (MODE >= Z_F
     zf v[G::PT];
 #pragma unroll
     for (int i = 0; i < G::PT && i * G::TL < N; ++i)
-      v[i] = live ? z2_to_zf(reinterpret_cast<const z2*>(in)[base + t + G::TL * i])
+      v[i] = live ? z2_to_zf(reinterpret_cast<const z2*>(in)[at(t + G::TL * i)])
                   : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     zf* hb = zs + (size_t)G::L * N + (size_t)g * G::HT;
     if (o.apply_h) {
@@ -458,8 +486,8 @@ __global__ void __launch_bounds__(ZGeo<N>::NT, ZGeo<N>::NT <= 256 ? (MODE >= Z_F
       zf w = v[i];
       if (o.apply_h) w = zf_mul(w, hb[kx <= N / 2 ? kx : N - kx]);
       if (o.kmask && live) w = zf_mul(w, z2_to_zf(zmask(o.kmask, o.kmask_type, line, kx, N)));
-      if (o.spectrum_out && live) o.spectrum_out[base + kx] = zf_to_z2(w);
-      buf[kx] = w;
+      if (o.spectrum_out && live) o.spectrum_out[at(kx)] = zf_to_z2(w);
+      buf[kx * LS] = w;
     }
   } else {
 #pragma unroll
@@ -468,21 +496,21 @@ __global__ void __launch_bounds__(ZGeo<N>::NT, ZGeo<N>::NT <= 256 ? (MODE >= Z_F
       zf v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
       if (live) {
         if constexpr (IN_D) {
-          v = z2_to_zf(reinterpret_cast<const z2*>(in)[base + x]);
+          v = z2_to_zf(reinterpret_cast<const z2*>(in)[at(x)]);
         } else {
-          v = reinterpret_cast<const zf*>(in)[base + x];
+          v = reinterpret_cast<const zf*>(in)[at(x)];
         }
       }
       if (MODE == Z_FWD && live && (o.lens || o.xmask) && !o.post)
-        v = zf_mul(v, zxmul_ff(o, line, x, N));
-      buf[x] = v;
+        v = zf_mul(v, COLS ? zxmul_ff(o, x, line, N) : zxmul_ff(o, line, x, N));
+      buf[x * LS] = v;
     }
   }
   __syncthreads();
   if constexpr (MODE == Z_INV || MODE == Z_KINV) {
-    zfft<N, 1>(buf, t, tw);
+    zfft<N, 1, LS>(buf, t, tw);
   } else {
-    zfft<N, -1>(buf, t, tw);
+    zfft<N, -1, LS>(buf, t, tw);
   }
   if constexpr (MODE == Z_FUSED) {
     // H of this line at |ky| = 0..N/2 once each (H(kx, ky) = H(kx, -ky))
@@ -497,73 +525,84 @@ __global__ void __launch_bounds__(ZGeo<N>::NT, ZGeo<N>::NT <= 256 ? (MODE >= Z_F
 #pragma unroll
     for (int i = 0; i < G::PT && i * G::TL < N; ++i) {
       const int ky = t + G::TL * i;
-      zf v = buf[ky];
+      zf v = buf[ky * LS];
       if (o.apply_h) v = zf_mul(v, hb[ky <= N / 2 ? ky : N - ky]);
       if (o.kmask && live) v = zf_mul(v, z2_to_zf(zmask(o.kmask, o.kmask_type, ky, line, N)));
       if (o.spectrum_out && live) o.spectrum_out[(size_t)ky * N + line] = zf_to_z2(v);
-      buf[ky] = zf_scale(v, o.scale_h, o.scale_l);
+      buf[ky * LS] = zf_scale(v, o.scale_h, o.scale_l);
     }
     __syncthreads();
-    zfft<N, 1>(buf, t, tw);
+    zfft<N, 1, LS>(buf, t, tw);
   }
   if (!live) return;
 #pragma unroll
   for (int i = 0; i < G::PT && i * G::TL < N; ++i) {
     const int x = t + G::TL * i;
-    zf v = buf[x];
+    zf v = buf[x * LS];
     if (MODE == Z_INV) {
       v = zf_scale(v, o.scale_h, o.scale_l);
-      if ((o.lens || o.xmask) && o.post) v = zf_mul(v, zxmul_ff(o, line, x, N));
+      if ((o.lens || o.xmask) && o.post)
+        v = zf_mul(v, COLS ? zxmul_ff(o, x, line, N) : zxmul_ff(o, line, x, N));
       if (o.iprofile) {
         float ah, al, bh, bl, ph, pl;
         ff_mul2(v.x, v.y, v.x, v.y, ah, al);
         ff_mul2(v.z, v.w, v.z, v.w, bh, bl);
         ff_add2(ah, al, bh, bl, ph, pl);
-        o.iprofile[base + x] = f2d(ph) + f2d(pl);
+        o.iprofile[at(x)] = f2d(ph) + f2d(pl);
       }
     }
     if constexpr (OUT_D) {
-      reinterpret_cast<z2*>(out)[base + x] = zf_to_z2(v);
+      reinterpret_cast<z2*>(out)[at(x)] = zf_to_z2(v);
     } else {
-      reinterpret_cast<zf*>(out)[base + x] = v;
+      reinterpret_cast<zf*>(out)[at(x)] = v;
     }
   }
 }
 
-// The line-pass variants a size uses: (mode, reads complex128, writes complex128).
-#define LP_ZLINE_VARIANTS(X) \
-  X(Z_FWD, true, false) X(Z_FWD, false, true) X(Z_INV, true, false) X(Z_INV, false, true) \
-  X(Z_FUSED, false, false) X(Z_KINV, true, false)
+// The line-pass variants a size uses: (mode, reads complex128, writes
+// complex128, column pass).  Column passes exist for N <= 4096 (two 8192
+// lines would need 2048 threads per CTA); 8192 transposes instead.
+#define LP_ZLINE_ROWS(X)                                                              \
+  X(Z_FWD, true, false, false) X(Z_FWD, false, true, false) X(Z_INV, true, false, false) \
+  X(Z_INV, false, true, false) X(Z_FUSED, false, false, false) X(Z_KINV, true, false, false)
+#define LP_ZLINE_COLS(X) \
+  X(Z_FWD, false, true, true) X(Z_INV, false, true, true) X(Z_FUSED, false, false, true)
 
 template <int N>
 cudaError_t set_smem() {
   cudaError_t e = cudaSuccess;
-#define LP_ZSET(M, I, O)                                                                  \
+#define LP_ZSET(M, I, O, C)                                                               \
   if (e == cudaSuccess)                                                                   \
-    e = cudaFuncSetAttribute(zline_kernel<N, M, I, O>,                                    \
+    e = cudaFuncSetAttribute(zline_kernel<N, M, I, O, C>,                                 \
                              cudaFuncAttributeMaxDynamicSharedMemorySize,                 \
-                             (int)(M >= Z_FUSED ? ZGeo<N>::SMEM_FUSED : ZGeo<N>::SMEM));
-  LP_ZLINE_VARIANTS(LP_ZSET)
+                             (int)(M >= Z_FUSED ? ZG<N, C>::SMEM_FUSED : ZG<N, C>::SMEM));
+  LP_ZLINE_ROWS(LP_ZSET)
+  if constexpr (N <= 4096) {
+    LP_ZLINE_COLS(LP_ZSET)
+  }
 #undef LP_ZSET
   return e;
 }
 
 template <int N>
-cudaError_t zline(int mode, bool in_d, bool out_d, const void* in, void* out, ZOps o,
+cudaError_t zline(int mode, bool in_d, bool out_d, bool cols, const void* in, void* out, ZOps o,
                   const zf* tw, cudaStream_t st) {
-  using G = ZGeo<N>;
-  const int grid = (N + G::L - 1) / G::L;
   const float sh = (float)o.scale;
   o.scale_h = sh;
   o.scale_l = (float)(o.scale - (double)sh);
   bool done = false;
-#define LP_ZLAUNCH(M, I, O)                                                                 \
-  if (!done && mode == M && in_d == I && out_d == O) {                                      \
-    zline_kernel<N, M, I, O>                                                                \
-        <<<grid, G::NT, M >= Z_FUSED ? G::SMEM_FUSED : G::SMEM, st>>>(in, out, o, tw);      \
+#define LP_ZLAUNCH(M, I, O, C)                                                              \
+  if (!done && mode == M && in_d == I && out_d == O && cols == C) {                         \
+    using G = ZG<N, C>;                                                                     \
+    zline_kernel<N, M, I, O, C><<<(N + G::L - 1) / G::L, G::NT,                             \
+                                  M >= Z_FUSED ? G::SMEM_FUSED : G::SMEM, st>>>(in, out, o, \
+                                                                                tw);        \
     done = true;                                                                            \
   }
-  LP_ZLINE_VARIANTS(LP_ZLAUNCH)
+  LP_ZLINE_ROWS(LP_ZLAUNCH)
+  if constexpr (N <= 4096) {
+    LP_ZLINE_COLS(LP_ZLAUNCH)
+  }
 #undef LP_ZLAUNCH
   return done ? cudaGetLastError() : cudaErrorInvalidValue;
 }

@@ -3,11 +3,11 @@
 
 namespace lp {
 
-cudaError_t zline_g1024_2048(int n, int mode, bool in_d, bool out_d, const void* in, void* out,
-                             const ZOps& o, const float4* tw, cudaStream_t st) {
+cudaError_t zline_g1024_2048(int n, int mode, bool in_d, bool out_d, bool cols, const void* in,
+                    void* out, const ZOps& o, const float4* tw, cudaStream_t st) {
   switch (n) {
-    case 1024: return zline<1024>(mode, in_d, out_d, in, out, o, tw, st);
-    case 2048: return zline<2048>(mode, in_d, out_d, in, out, o, tw, st);
+    case 1024: return zline<1024>(mode, in_d, out_d, cols, in, out, o, tw, st);
+    case 2048: return zline<2048>(mode, in_d, out_d, cols, in, out, o, tw, st);
     default: return cudaErrorInvalidValue;
   }
 }

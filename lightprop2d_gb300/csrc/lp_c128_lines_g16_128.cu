@@ -3,13 +3,13 @@
 
 namespace lp {
 
-cudaError_t zline_g16_128(int n, int mode, bool in_d, bool out_d, const void* in, void* out,
-                          const ZOps& o, const float4* tw, cudaStream_t st) {
+cudaError_t zline_g16_128(int n, int mode, bool in_d, bool out_d, bool cols, const void* in,
+                    void* out, const ZOps& o, const float4* tw, cudaStream_t st) {
   switch (n) {
-    case 16: return zline<16>(mode, in_d, out_d, in, out, o, tw, st);
-    case 32: return zline<32>(mode, in_d, out_d, in, out, o, tw, st);
-    case 64: return zline<64>(mode, in_d, out_d, in, out, o, tw, st);
-    case 128: return zline<128>(mode, in_d, out_d, in, out, o, tw, st);
+    case 16: return zline<16>(mode, in_d, out_d, cols, in, out, o, tw, st);
+    case 32: return zline<32>(mode, in_d, out_d, cols, in, out, o, tw, st);
+    case 64: return zline<64>(mode, in_d, out_d, cols, in, out, o, tw, st);
+    case 128: return zline<128>(mode, in_d, out_d, cols, in, out, o, tw, st);
     default: return cudaErrorInvalidValue;
   }
 }

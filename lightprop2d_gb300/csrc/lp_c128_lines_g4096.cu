@@ -3,10 +3,10 @@
 
 namespace lp {
 
-cudaError_t zline_g4096(int n, int mode, bool in_d, bool out_d, const void* in, void* out,
-                        const ZOps& o, const float4* tw, cudaStream_t st) {
+cudaError_t zline_g4096(int n, int mode, bool in_d, bool out_d, bool cols, const void* in,
+                    void* out, const ZOps& o, const float4* tw, cudaStream_t st) {
   switch (n) {
-    case 4096: return zline<4096>(mode, in_d, out_d, in, out, o, tw, st);
+    case 4096: return zline<4096>(mode, in_d, out_d, cols, in, out, o, tw, st);
     default: return cudaErrorInvalidValue;
   }
 }
