@@ -14,29 +14,33 @@
 // Magnitudes below ~2^-100 lose their low half and below 2^-126 flush to
 // zero (FP32's exponent range).
 //
-// A 2-D transform is a line pass over rows, an in-place square transpose, a
-// line pass over the (former) columns and a transpose back.  A line pass
-// holds whole lines in shared memory (N <= 8192: at most 128 KB) and
-// transforms them with a Stockham sequence of radix-4 stages (one radix-2
-// stage first when log2 N is odd): each thread keeps 8 points in registers
-// between the read and write halves of a stage, so the line is transformed
-// in place (8 rather than 16 points a thread: 64 registers, four 256-thread
-// CTAs per SM; 0.44 against 0.52 ms per 2048^2 propagate, and 4 points a
-// thread measured 0.49).  Stage twiddles come from a per-size table W_N^k (k < N) computed
-// on the host in double and split into float-float.  Intermediate grids
-// between the passes hold float-float values (16 bytes a point, like a
-// complex128); the first pass reads the caller's complex128 and the last
-// writes complex128.
+// A 2-D transform is a line pass over rows and a line pass over columns.  A
+// line pass holds whole lines in shared memory (N <= 8192: at most 128 KB)
+// and transforms them with a Stockham sequence of radix-4 stages (one
+// radix-2 stage first when log2 N is odd): each thread keeps 8 points in
+// registers between the read and write halves of a stage, so the line is
+// transformed in place (8 rather than 16 points a thread: 64 registers, four
+// 256-thread CTAs per SM; 0.44 against 0.52 ms per 2048^2 propagate, and 4
+// points a thread measured 0.49).  A column pass takes two adjacent columns
+// per CTA, so a warp's loads cover whole 32-byte sectors, and reads the grid
+// in place; at 8192 (two lines would need 2048 threads) the grid is
+// transposed in place around a row pass instead.  Stage twiddles come from a
+// per-size table W_N^k (k < N) computed on the host in double and split into
+// float-float.  Intermediate grids between the passes hold float-float
+// values (16 bytes a point, like a complex128); the first pass reads the
+// caller's complex128 and the last writes complex128.
 //
 // A propagate is
 //   rows:     [x-domain multipliers] forward FFT
-//   transpose
-//   lines:    forward FFT, H(z) = exp(2*pi*i*(trunc(Kz z) - Kz z)) with Kz in
+//   columns:  forward FFT, H(z) = exp(2*pi*i*(trunc(Kz z) - Kz z)) with Kz in
 //             float64 exactly as beam2d.py:305-308 and :485-489 compute it
 //             (once per |ky|: H(kx, ky) = H(kx, -ky)), k-domain mask, 1/N^2,
 //             inverse FFT
-//   transpose
 //   rows:     inverse FFT, |field|^2 epilogue (float64)
+// and a propagate of a stored spectrum (Beam2D.propagate) is
+//   rows:     H(z) and k-domain mask as each spectrum row loads (once per
+//             |kx|), [multiplied spectrum written back], inverse FFT
+//   columns:  inverse FFT, 1/N^2
 // Sizes that are not powers of two use Bluestein's algorithm (as the
 // complex64 path does, lp_bluestein.cu) on a per-stream work grid.
 #include <cuda_runtime.h>
