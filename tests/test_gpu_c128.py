@@ -38,7 +38,30 @@ def test_fft2_c128(n):
     assert O.rel_l2(H(B.ifft2(f)), x) < TOL128
 
 
-@pytest.mark.parametrize("n,area,z", [(256, 0.05, 0.7), (100, 0.03, 0.2), (1024, 0.2, 3.0)])
+@pytest.mark.parametrize("n", [4096, 8192])
+def test_fft2_c128_large_plane_wave_and_round_trip(n):
+    """4096 (in-place column pass with 1024-thread CTAs) and 8192 (transposes
+    around a row pass): the transform of a plane wave is N^2 at its
+    frequency and zero elsewhere, and ifft2(fft2(x)) returns x."""
+    from lightprop2d_gb300 import backend as B
+    a, b = 37, n - 5
+    iy, ix = torch.meshgrid(torch.arange(n, dtype=torch.float64, device="cuda"),
+                            torch.arange(n, dtype=torch.float64, device="cuda"), indexing="ij")
+    x = torch.polar(torch.ones_like(iy), 2 * np.pi * ((a * iy + b * ix) % n) / n)
+    f = B.fft2(x)
+    peak = complex(f[a, b])
+    assert abs(peak - n * n) < 1e-10 * n * n
+    f[a, b] = 0
+    assert float(torch.linalg.vector_norm(f)) < 1e-11 * n * n
+    del f
+    rng = np.random.default_rng(n)
+    y = torch.as_tensor(rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n)), device="cuda")
+    back = B.ifft2(B.fft2(y))
+    assert float(torch.linalg.vector_norm(back - y) / torch.linalg.vector_norm(y)) < TOL128
+
+
+@pytest.mark.parametrize("n,area,z", [(256, 0.05, 0.7), (100, 0.03, 0.2), (1024, 0.2, 3.0),
+                                      (4096, 0.4, 2.0)])
 def test_propagate_field_c128_with_every_multiplier(n, area, z):
     from lightprop2d_gb300 import backend as B
     wl = 632 * nm
