@@ -89,6 +89,8 @@ struct ZGeo {
   static constexpr int HT = N / 2 + 1;                   // H table entries per line
   static constexpr size_t SMEM = 16 * (size_t)L * N;
   static constexpr size_t SMEM_FUSED = 16 * (size_t)L * (N + HT);
+  // first row pass: the lens's x factors over |x - N/2| and one y factor a line
+  static constexpr size_t SMEM_FWD = 16 * ((size_t)L * N + HT + L);
   static constexpr int LOG = N == 16 ? 4 : N == 32 ? 5 : N == 64 ? 6 : N == 128 ? 7
                            : N == 256 ? 8 : N == 512 ? 9 : N == 1024 ? 10 : N == 2048 ? 11
                            : N == 4096 ? 12 : 13;
@@ -328,6 +330,19 @@ __device__ __forceinline__ zf zxmul_ff(const ZOps& o, int y, int x, int n) {
   return m;
 }
 
+// cos + i sin of lens_c * u^2 (u = j dL: one coordinate of the reference's
+// lens phase, beam2d.py:508-510), the phase in FP64 turned into turns by the
+// double-double 1/(2 pi).  exp(i c (X^2 + Y^2)) is the product of the x and
+// y factors (which rounds differently from one float64 phase by ~1e-16 of
+// the phase).
+__device__ __forceinline__ zf zlens_axis(const ZOps& o, int j) {
+  const double u = (double)j * o.dL;
+  const double ph = (u * u) * o.lens_c;
+  const double p = ph * kInv2PiH;
+  const double e = fma(ph, kInv2PiH, -p) + ph * kInv2PiL;
+  return zcis_2pi((p - rint(p)) + e);
+}
+
 // k-domain multiplier at (ky, kx) as float-float: H as zh_value computes it
 // (the reference's float64 Kz and phase), times the mask.
 __device__ __forceinline__ zf zkmul_ff(const ZOps& o, int ky, int kx, int n) {
@@ -436,7 +451,10 @@ using ZG = ZGeo<N, COLS ? 2 : 1>;
 template <int N, int MODE, bool COLS>
 constexpr int zmin_blocks() {
   constexpr int nt = ZG<N, COLS>::NT;
-  return nt <= 256 ? (MODE >= Z_FUSED ? 3 : 4) : (nt <= 512 ? 2 : 1);
+  // 64 registers (four CTAs a SM) for the plain passes; the passes with H
+  // or lens tables take 85 (three)
+  constexpr bool tables = MODE >= Z_FUSED || (MODE == Z_FWD && !COLS);
+  return nt <= 256 ? (tables ? 3 : 4) : (nt <= 512 ? 2 : 1);
 }
 
 // One line pass over N lines.  Rows (COLS false): line = row, element x at
@@ -488,6 +506,30 @@ __global__ void __launch_bounds__(ZG<N, COLS>::NT, zmin_blocks<N, MODE, COLS>())
       if (o.kmask && live) w = zf_mul(w, z2_to_zf(zmask(o.kmask, o.kmask_type, line, kx, N)));
       if (o.spectrum_out && live) o.spectrum_out[at(kx)] = zf_to_z2(w);
       buf[kx * LS] = w;
+    }
+  } else if constexpr (MODE == Z_FWD && !COLS && IN_D) {
+    // first row pass: loads in flight while the lens's x factors over
+    // |x - N/2| (shared by the CTA's lines) and each line's y factor fill
+    zf v[G::PT];
+#pragma unroll
+    for (int i = 0; i < G::PT && i * G::TL < N; ++i)
+      v[i] = live ? z2_to_zf(reinterpret_cast<const z2*>(in)[at(t + G::TL * i)])
+                  : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const bool lens = o.lens && !o.post;
+    zf* lt = zs + (size_t)G::L * N;  // [0, HT): x factors; [HT + g]: line g's y factor
+    if (lens) {
+      for (int j = threadIdx.x; j < G::HT; j += G::NT) lt[j] = zlens_axis(o, j);
+      if (t == 0) lt[G::HT + g] = zlens_axis(o, abs(line - N / 2));
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < G::PT && i * G::TL < N; ++i) {
+      const int x = t + G::TL * i;
+      zf w = v[i];
+      if (lens && live) w = zf_mul(zf_mul(w, lt[abs(x - N / 2)]), lt[G::HT + g]);
+      if (o.xmask && live && !o.post)
+        w = zf_mul(w, z2_to_zf(zmask(o.xmask, o.xmask_type, line, x, N)));
+      buf[x * LS] = w;
     }
   } else {
 #pragma unroll
@@ -568,6 +610,14 @@ __global__ void __launch_bounds__(ZG<N, COLS>::NT, zmin_blocks<N, MODE, COLS>())
 #define LP_ZLINE_COLS(X) \
   X(Z_FWD, false, true, true) X(Z_INV, false, true, true) X(Z_FUSED, false, false, true)
 
+// Dynamic shared memory of a pass: lines, plus the H table (fused, k-first
+// passes) or the lens tables (first row pass).
+template <int N, int M, bool I, bool C>
+constexpr size_t zsmem_bytes() {
+  using G = ZG<N, C>;
+  return M >= Z_FUSED ? G::SMEM_FUSED : (M == Z_FWD && !C && I) ? G::SMEM_FWD : G::SMEM;
+}
+
 template <int N>
 cudaError_t set_smem() {
   cudaError_t e = cudaSuccess;
@@ -575,7 +625,7 @@ cudaError_t set_smem() {
   if (e == cudaSuccess)                                                                   \
     e = cudaFuncSetAttribute(zline_kernel<N, M, I, O, C>,                                 \
                              cudaFuncAttributeMaxDynamicSharedMemorySize,                 \
-                             (int)(M >= Z_FUSED ? ZG<N, C>::SMEM_FUSED : ZG<N, C>::SMEM));
+                             (int)zsmem_bytes<N, M, I, C>());
   LP_ZLINE_ROWS(LP_ZSET)
   if constexpr (N <= 4096) {
     LP_ZLINE_COLS(LP_ZSET)
@@ -594,9 +644,8 @@ cudaError_t zline(int mode, bool in_d, bool out_d, bool cols, const void* in, vo
 #define LP_ZLAUNCH(M, I, O, C)                                                              \
   if (!done && mode == M && in_d == I && out_d == O && cols == C) {                         \
     using G = ZG<N, C>;                                                                     \
-    zline_kernel<N, M, I, O, C><<<(N + G::L - 1) / G::L, G::NT,                             \
-                                  M >= Z_FUSED ? G::SMEM_FUSED : G::SMEM, st>>>(in, out, o, \
-                                                                                tw);        \
+    zline_kernel<N, M, I, O, C><<<(N + G::L - 1) / G::L, G::NT, zsmem_bytes<N, M, I, C>(),  \
+                                  st>>>(in, out, o, tw);                                    \
     done = true;                                                                            \
   }
   LP_ZLINE_ROWS(LP_ZLAUNCH)
