@@ -531,6 +531,24 @@ __global__ void __launch_bounds__(ZG<N, COLS>::NT, zmin_blocks<N, MODE, COLS>())
         w = zf_mul(w, z2_to_zf(zmask(o.xmask, o.xmask_type, line, x, N)));
       buf[x * LS] = w;
     }
+  } else if constexpr (MODE == Z_FUSED) {
+    // loads in flight while the H of this line (kx = line) at |ky| =
+    // 0..N/2 fills once each (H(kx, ky) = H(kx, -ky)); the table is read
+    // after the forward transform's barriers
+    zf v[G::PT];
+#pragma unroll
+    for (int i = 0; i < G::PT && i * G::TL < N; ++i)
+      v[i] = live ? reinterpret_cast<const zf*>(in)[at(t + G::TL * i)]
+                  : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (o.apply_h) {
+      zf* hb = zs + (size_t)G::L * N + (size_t)g * G::HT;
+      const int h = (N + 1) / 2;
+      const double fx = (double)(line < h ? line : line - N) * o.val;
+      const double a = o.k0 * o.k0 - fx * fx;
+      for (int j = t; j < G::HT; j += G::TL) hb[j] = zh_value(o, a, j);
+    }
+#pragma unroll
+    for (int i = 0; i < G::PT && i * G::TL < N; ++i) buf[(t + G::TL * i) * LS] = v[i];
   } else {
 #pragma unroll
     for (int i = 0; i < G::PT && i * G::TL < N; ++i) {
@@ -555,15 +573,7 @@ __global__ void __launch_bounds__(ZG<N, COLS>::NT, zmin_blocks<N, MODE, COLS>())
     zfft<N, -1, LS>(buf, t, tw);
   }
   if constexpr (MODE == Z_FUSED) {
-    // H of this line at |ky| = 0..N/2 once each (H(kx, ky) = H(kx, -ky))
-    zf* hb = zs + (size_t)G::L * N + (size_t)g * G::HT;
-    if (o.apply_h) {
-      const int h = (N + 1) / 2;
-      const double fx = (double)(line < h ? line : line - N) * o.val;
-      const double a = o.k0 * o.k0 - fx * fx;
-      for (int j = t; j < G::HT; j += G::TL) hb[j] = zh_value(o, a, j);
-    }
-    __syncthreads();
+    const zf* hb = zs + (size_t)G::L * N + (size_t)g * G::HT;
 #pragma unroll
     for (int i = 0; i < G::PT && i * G::TL < N; ++i) {
       const int ky = t + G::TL * i;
