@@ -38,15 +38,30 @@
 // 1: load the next tile into a second register set while transforming the
 // current one; 0: load it at the top of the next iteration.
 #ifndef LP_ROW_PREFETCH
-#define LP_ROW_PREFETCH (LP_N < 8192)
+#define LP_ROW_PREFETCH (LP_N < 8192 && LP_N != 1024)
 #endif
 #ifndef LP_COL_PREFETCH
 #define LP_COL_PREFETCH 0
 #endif
 // Minimum resident CTAs per SM requested from the register allocator
 // (2 with 512-thread column CTAs caps them at 64 registers).
+//
+// Row passes at 1024-2048 run one- or two-row CTAs of 128 threads, several
+// per SM: a CTA's barriers then hold only its own rows, so one CTA's loads,
+// exchanges and barrier waits overlap another's arithmetic.  Measured on
+// GB300 (back-to-back fused propagates, inputs larger than L2): 2048^2 with
+// three 170-register CTAs per SM and next-row prefetch 63.2 us, against
+// 65.8 us for one 256-thread CTA (two rows, 225 registers) per SM, 63.6 us
+// with two CTAs per SM, 64.1 us with four, 64.9-66.0 us without prefetch at
+// three to five; 1024^2 with four 128-register CTAs per SM without prefetch
+// 20.5 us, against 22.2 us for one 256-thread CTA (four rows) per SM and
+// 21.3-22.5 us for 64-thread one-row CTAs or 128-thread CTAs with prefetch.
 #ifndef LP_ROW_MINB
-#define LP_ROW_MINB 1
+#define LP_ROW_MINB (LP_N == 2048 ? 3 : LP_N == 1024 ? 4 : 1)
+#endif
+// Threads per row-kernel CTA for N >= 1024 (whole rows per CTA).
+#ifndef LP_ROW_THREADS
+#define LP_ROW_THREADS (LP_N == 2048 || LP_N == 1024 ? 128 : 256)
 #endif
 #ifndef LP_COL_MINB
 #define LP_COL_MINB (LP_N >= 2048 ? 1 : 2)
@@ -80,8 +95,8 @@ namespace {
 template <int N>
 struct Geo : FftGeo<N> {
   using F = FftGeo<N>;
-  // rows per CTA: 256 threads for large N, one warp's worth for small N
-  static constexpr int ROWS = N >= 1024 ? cmax(1, 256 / F::T) : cmin(N, cmax(1, 32 / F::T));
+  // rows per CTA: LP_ROW_THREADS threads for large N, one warp's worth for small N
+  static constexpr int ROWS = N >= 1024 ? cmax(1, LP_ROW_THREADS / F::T) : cmin(N, cmax(1, 32 / F::T));
   // columns per CTA: at least 4 so every row segment is a full 32-byte sector
   static constexpr int COLS = N >= 8192   ? LP_COL_C8192
                               : N >= 4096 ? LP_COL_C4096
