@@ -204,6 +204,10 @@ __device__ __forceinline__ void fft_rest(float2 (&v)[16], float2* buf, const flo
   if constexpr (FftGeo<N>::NST >= 4) fft_stage<N, S, 3, IL, LINES, SY>(v, buf, tw, t, line);
 }
 
+// Column mode of the size kernels only: COL_FUSED with H and the scale as
+// the only spectral multipliers (the launcher picks it when ops allow).
+constexpr int COL_FUSED_LEAN = 3;
+
 struct NoHook {
   __device__ __forceinline__ void operator()() const {}
 };
@@ -429,12 +433,12 @@ __device__ __forceinline__ void row_tile(float2 (&v)[16], float2* out, int tile,
 // Spectral multiplier without the mask at (qx = sx^2, qy = sy^2): H(z)
 // [* d/dz factor].  (a_hi, a_lo) = 1 - beta*qx, the column constant of the
 // float-float phase (unused by the plain-FP32 variant).
-template <int N>
+template <int N, bool LEAN = false>
 __device__ __forceinline__ float2 transfer_value_cc(float qx, float a_hi, float a_lo, float qy,
                                                     const ColOps& ops) {
   bool evan;
   float sv, f;
-  if (ops.phase_fp32) {
+  if (!LEAN && ops.phase_fp32) {
     f = kz_phase_f32(ops.kp, qx, qy, evan, sv);
   } else {
     f = kz_phase_ff(ops.kp, a_hi, a_lo, qy, evan, sv);
@@ -442,7 +446,7 @@ __device__ __forceinline__ float2 transfer_value_cc(float qx, float a_hi, float 
   // H = exp(-2*pi*i*f); the adjoint uses conj(H).
   float2 m = cis_cycles(f, ops.conj ? 1.0f : -1.0f);
   if (evan) m = ops.evan_mask ? make_float2(0.0f, 0.0f) : make_float2(1.0f, 0.0f);
-  if (ops.dz) {
+  if (!LEAN && ops.dz) {
     // d/dz exp(-2*pi*i*kz*z) = -2*pi*i*kz * H with kz = k0*sqrt(v).
     const float gz = ops.kp.two_pi_k0 * sv * (ops.conj ? 1.0f : -1.0f);
     m = make_float2(-gz * m.y, gz * m.x);
@@ -465,12 +469,34 @@ __device__ __forceinline__ float2 transfer_value(int sy_abs, int sx, const ColOp
 // then each point reads its entry.  Table entry (a, cc) sits at a*C + cc and
 // thread tid fills column tid % C, so each thread computes its column's
 // float-float constant once.  The buffer must be free on entry; it is in use
-// on exit (callers sync before the next transform).
-template <int N, int C, int SY = 1>
+// on exit (callers sync before the next transform).  LEAN: H with the scale
+// folded into the table, and no k mask, spectrum write, d/dz or plain-FP32
+// phase (the caller checks ops for these).
+template <int N, int C, int SY = 1, bool LEAN = false>
 __device__ __forceinline__ void apply_spectral(float2 (&v)[16], float2* tab, int x0, int c, int t,
                                                const ColOps& ops) {
   constexpr int T = FftGeo<N>::T, NT = C * T, HE = N / 2 + 1;
   const int kx = x0 + c;
+  if constexpr (LEAN) {
+    const int tid = group_tid<SY>();
+    const int cc = tid % C, x = x0 + cc;
+    const int sx = x < N / 2 ? x : x - N;
+    const float qx = (float)(sx * sx);
+    float a_hi, a_lo;
+    column_constant(ops.kp, qx, a_hi, a_lo);
+#pragma unroll 1
+    for (int a = tid / C; a < HE; a += NT / C)
+      tab[a * C + cc] = cscale(transfer_value_cc<N, true>(qx, a_hi, a_lo, (float)(a * a), ops),
+                               ops.scale);
+    group_sync<SY>();
+    static_for<16>([&](auto jc) {
+      constexpr int j = decltype(jc)::value;
+      const int ky = t + T * j;
+      const int a = ky <= N / 2 ? ky : N - ky;
+      v[j] = cmul(v[j], tab[a * C + c]);
+    });
+    return;
+  }
   if (ops.apply_h) {
     const int tid = group_tid<SY>();
     const int cc = tid % C, x = x0 + cc;
@@ -515,7 +541,8 @@ __device__ __forceinline__ void load_col(float2 (&v)[16], const float2* in, int 
 // exchange group (SY), thread (c = tid % C, t = tid / C).  MODE: COL_FWD forward
 // transform; COL_INV spectral multiply then inverse transform; COL_FUSED
 // forward, spectral multiply, inverse (one copy of the transform code:
-// inverse(x) = conj(forward(conj(x)))).  v holds the thread's loaded points;
+// inverse(x) = conj(forward(conj(x)))); COL_FUSED_LEAN the same with H and
+// the scale only (apply_spectral's LEAN form).  v holds the thread's loaded points;
 // `after_first` runs after the first stage of the first transform and
 // `before_store` after the last stage has read the buffer into registers.
 // The buffer (C * BUF float2) must be free on entry; callers sync the group
@@ -546,7 +573,7 @@ __device__ __forceinline__ void col_tile(float2 (&v)[16], float2* out, int tile,
       fft_rest<N, -1, true, C, SY>(v, buf, tw, t, c);
       if (pass == 0) {
         group_sync<SY>();
-        apply_spectral<N, C, SY>(v, buf, x0, c, t, ops);
+        apply_spectral<N, C, SY, MODE == COL_FUSED_LEAN>(v, buf, x0, c, t, ops);
         group_sync<SY>();
         conj16(v);
       }

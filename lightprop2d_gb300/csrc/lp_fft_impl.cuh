@@ -78,6 +78,12 @@
 #ifndef LP_COL_TMA
 #define LP_COL_TMA 0
 #endif
+// 1: fused column passes whose only spectral multipliers are H and the scale
+// run a kernel built for that case (no k-mask, spectrum-write or d/dz code;
+// the scale folded into the H table).
+#ifndef LP_COL_LEAN
+#define LP_COL_LEAN 1
+#endif
 // Preferred shared-memory carveout (percent) of every pass kernel of this
 // size; -1 leaves the driver's default.
 #ifndef LP_CARVEOUT
@@ -449,6 +455,11 @@ cudaError_t init_size() {
     e = cudaFuncSetAttribute(col_kernel<N, COL_INV>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(col_kernel<N, COL_FUSED>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+#if LP_COL_LEAN
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(col_kernel<N, COL_FUSED_LEAN>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+#endif
 #if LP_CARVEOUT >= 0
   for (const void* k : {(const void*)row_kernel<N, -1>, (const void*)row_kernel<N, 1>,
                         (const void*)col_kernel<N, COL_FWD>, (const void*)col_kernel<N, COL_INV>,
@@ -520,6 +531,11 @@ cudaError_t launch_col(int mode, const float2* in, float2* out, const ColOps& op
 #endif
   const int grid = grid_for(Geo<N>::COL_UNITS, g_occ_col, g_ctas_col);
   const size_t sm = Geo<N>::COL_SMEM;
+#if LP_COL_LEAN
+  if (mode == COL_FUSED && ops.apply_h && !ops.kmask && !ops.spectrum_out && !ops.dz &&
+      !ops.phase_fp32)
+    return launch_pdl(col_kernel<N, COL_FUSED_LEAN>, grid, bs, sm, st, in, out, ops);
+#endif
   switch (mode) {
     case COL_FWD: return launch_pdl(col_kernel<N, COL_FWD>, grid, bs, sm, st, in, out, ops);
     case COL_INV: return launch_pdl(col_kernel<N, COL_INV>, grid, bs, sm, st, in, out, ops);
