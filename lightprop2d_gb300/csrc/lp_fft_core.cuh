@@ -204,9 +204,11 @@ __device__ __forceinline__ void fft_rest(float2 (&v)[16], float2* buf, const flo
   if constexpr (FftGeo<N>::NST >= 4) fft_stage<N, S, 3, IL, LINES, SY>(v, buf, tw, t, line);
 }
 
-// Column mode of the size kernels only: COL_FUSED with H and the scale as
-// the only spectral multipliers (the launcher picks it when ops allow).
+// Column modes of the size kernels only: COL_FUSED / COL_INV with H and the
+// scale as the only spectral multipliers (the launcher picks them when ops
+// allow).
 constexpr int COL_FUSED_LEAN = 3;
+constexpr int COL_INV_LEAN = 4;
 
 struct NoHook {
   __device__ __forceinline__ void operator()() const {}
@@ -388,11 +390,12 @@ __device__ __forceinline__ void tile_moments(const float2 (&v)[16], int y, int t
 
 // Row tile: rows tile*L .. tile*L+L-1 by the first L*T threads of the
 // exchange group (SY: the CTA, or a 256-thread group), thread (line
-// g = tid / T, t = tid % T).  v holds the thread's loaded points of row
+// g = tid / T, t = tid % T).  LEAN: the transform alone (no multipliers,
+// scale or epilogue; the caller checks ops).  v holds the thread's loaded points of row
 // tile*L + g; `after_first` runs after the first stage (the per-size kernels
 // prefetch the next tile there).  The exchange buffer (L * BUF floats2) must
 // be free on entry.
-template <int N, int S, int L, int NT, bool CG, int SY = 1, class Hook>
+template <int N, int S, int L, int NT, bool CG, int SY = 1, class Hook, bool LEAN = false>
 __device__ __forceinline__ void row_tile(float2 (&v)[16], float2* out, int tile, const RowOps& ops,
                                          float2* buf, const float2* tw, Hook after_first) {
   constexpr int T = FftGeo<N>::T;
@@ -400,6 +403,14 @@ __device__ __forceinline__ void row_tile(float2 (&v)[16], float2* out, int tile,
   const int tid = group_tid<SY>();
   const int g = tid / T, t = tid % T;
   const int y = tile * L + g;
+  if constexpr (LEAN) {  // transform only (the caller checked ops)
+    fft_first<N, S, false, L>(v, buf, t, g);
+    after_first();
+    fft_rest<N, S, false, L, LS>(v, buf, tw, t, g);
+    float2* dst = out + (size_t)y * N + t;
+    static_for<16>([&](auto jc) { gst<CG>(dst + T * decltype(jc)::value, v[decltype(jc)::value]); });
+    return;
+  }
   const bool xops = ops.lens || ops.xmask;
   if (xops && !ops.x_at_store) {
     apply_xops<N, SY>(v, buf, NT, y, t, ops);
@@ -541,8 +552,8 @@ __device__ __forceinline__ void load_col(float2 (&v)[16], const float2* in, int 
 // exchange group (SY), thread (c = tid % C, t = tid / C).  MODE: COL_FWD forward
 // transform; COL_INV spectral multiply then inverse transform; COL_FUSED
 // forward, spectral multiply, inverse (one copy of the transform code:
-// inverse(x) = conj(forward(conj(x)))); COL_FUSED_LEAN the same with H and
-// the scale only (apply_spectral's LEAN form).  v holds the thread's loaded points;
+// inverse(x) = conj(forward(conj(x)))); COL_FUSED_LEAN / COL_INV_LEAN the
+// same with H and the scale only (apply_spectral's LEAN form).  v holds the thread's loaded points;
 // `after_first` runs after the first stage of the first transform and
 // `before_store` after the last stage has read the buffer into registers.
 // The buffer (C * BUF float2) must be free on entry; callers sync the group
@@ -559,8 +570,8 @@ __device__ __forceinline__ void col_tile(float2 (&v)[16], float2* out, int tile,
     fft_first<N, -1, true, C>(v, buf, t, c);
     after_first();
     fft_rest<N, -1, true, C, SY>(v, buf, tw, t, c);
-  } else if constexpr (MODE == COL_INV) {
-    apply_spectral<N, C, SY>(v, buf, x0, c, t, ops);
+  } else if constexpr (MODE == COL_INV || MODE == COL_INV_LEAN) {
+    apply_spectral<N, C, SY, MODE == COL_INV_LEAN>(v, buf, x0, c, t, ops);
     group_sync<SY>();
     fft_first<N, 1, true, C>(v, buf, t, c);
     after_first();

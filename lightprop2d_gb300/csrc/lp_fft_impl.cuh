@@ -84,6 +84,11 @@
 #ifndef LP_COL_LEAN
 #define LP_COL_LEAN 1
 #endif
+// 1: row passes with no multiplier, scale or epilogue run a kernel built for
+// the transform alone.
+#ifndef LP_ROW_LEAN
+#define LP_ROW_LEAN 1
+#endif
 // Preferred shared-memory carveout (percent) of every pass kernel of this
 // size; -1 leaves the driver's default.
 #ifndef LP_CARVEOUT
@@ -129,7 +134,7 @@ __device__ __forceinline__ void load_twiddles(float2* dst) {
   for (int i = threadIdx.x; i < FftGeo<LP_N>::TW_SIZE; i += NT) dst[i] = g_tw[i];
 }
 
-template <int N, int S>
+template <int N, int S, bool LEAN = false>
 __global__ void __launch_bounds__(Geo<N>::ROW_THREADS, LP_ROW_MINB)
     row_kernel(const float2* in, float2* out, RowOps ops) {
   constexpr int T = Geo<N>::T, L = Geo<N>::ROWS, NU = Geo<N>::ROW_UNITS;
@@ -154,12 +159,13 @@ __global__ void __launch_bounds__(Geo<N>::ROW_THREADS, LP_ROW_MINB)
 #endif
     __syncthreads();  // buffer free: previous tile's last-stage reads are done
 #if LP_ROW_PREFETCH
-    row_tile<N, S, L, NT, false>(v, out, tile, ops, smem, tw, [&] {
+    auto pf = [&] {
       if (next < NU) load_row<N>(p, in, next * L + g, t);
-    });
+    };
+    row_tile<N, S, L, NT, false, 1, decltype(pf), LEAN>(v, out, tile, ops, smem, tw, pf);
     static_for<16>([&](auto jc) { v[decltype(jc)::value] = p[decltype(jc)::value]; });
 #else
-    row_tile<N, S, L, NT, false>(v, out, tile, ops, smem, tw, NoHook{});
+    row_tile<N, S, L, NT, false, 1, NoHook, LEAN>(v, out, tile, ops, smem, tw, NoHook{});
 #endif
     tile = next;
   }
@@ -459,6 +465,15 @@ cudaError_t init_size() {
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(col_kernel<N, COL_FUSED_LEAN>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(col_kernel<N, COL_INV_LEAN>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
+#endif
+#if LP_ROW_LEAN
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(row_kernel<N, -1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(row_kernel<N, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs);
 #endif
 #if LP_CARVEOUT >= 0
   for (const void* k : {(const void*)row_kernel<N, -1>, (const void*)row_kernel<N, 1>,
@@ -503,6 +518,15 @@ cudaError_t launch_row(int inverse, const float2* in, float2* out, const RowOps&
   }
 #endif
   const int grid = grid_for(Geo<N>::ROW_UNITS, g_occ_row, g_ctas_row);
+#if LP_ROW_LEAN
+  if (!ops.lens && !ops.xmask && ops.scale == 1.0f && !ops.iprofile && !ops.moments) {
+    if (inverse)
+      return launch_pdl(row_kernel<N, 1, true>, grid, Geo<N>::ROW_THREADS, Geo<N>::ROW_SMEM, st,
+                        in, out, ops);
+    return launch_pdl(row_kernel<N, -1, true>, grid, Geo<N>::ROW_THREADS, Geo<N>::ROW_SMEM, st,
+                      in, out, ops);
+  }
+#endif
   if (inverse)
     return launch_pdl(row_kernel<N, 1>, grid, Geo<N>::ROW_THREADS, Geo<N>::ROW_SMEM, st, in, out,
                       ops);
@@ -532,9 +556,12 @@ cudaError_t launch_col(int mode, const float2* in, float2* out, const ColOps& op
   const int grid = grid_for(Geo<N>::COL_UNITS, g_occ_col, g_ctas_col);
   const size_t sm = Geo<N>::COL_SMEM;
 #if LP_COL_LEAN
-  if (mode == COL_FUSED && ops.apply_h && !ops.kmask && !ops.spectrum_out && !ops.dz &&
-      !ops.phase_fp32)
-    return launch_pdl(col_kernel<N, COL_FUSED_LEAN>, grid, bs, sm, st, in, out, ops);
+  if (ops.apply_h && !ops.kmask && !ops.spectrum_out && !ops.dz && !ops.phase_fp32) {
+    if (mode == COL_FUSED)
+      return launch_pdl(col_kernel<N, COL_FUSED_LEAN>, grid, bs, sm, st, in, out, ops);
+    if (mode == COL_INV)
+      return launch_pdl(col_kernel<N, COL_INV_LEAN>, grid, bs, sm, st, in, out, ops);
+  }
 #endif
   switch (mode) {
     case COL_FWD: return launch_pdl(col_kernel<N, COL_FWD>, grid, bs, sm, st, in, out, ops);
