@@ -30,6 +30,12 @@
 
 using namespace lp;
 
+// 1: column items of beams whose column ops are H and the scale only run the
+// column tile built for that case (no k-mask, spectrum-write or d/dz code).
+#ifndef LP_BATCH_COL_LEAN
+#define LP_BATCH_COL_LEAN 1
+#endif
+
 namespace {
 
 constexpr int kBT = 256;          // threads per CTA
@@ -53,6 +59,7 @@ struct BeamRec {
   float2* field;
   int n;
   int need1, need2;  // completed tiles needed before pass 1 / pass 2
+  int col_lean;      // column ops are H and the scale only (COL_FUSED_LEAN)
   RowOps fwd;
   ColOps col;
   RowOps inv;
@@ -87,7 +94,10 @@ __device__ __forceinline__ void run_tiles(const Item& item, const BeamRec* bp, f
     if (item.pass == 1) {
       const ColOps ops = bp->col;
       load_col<N, true>(v, field, tile * G::C + threadIdx.x % G::C, threadIdx.x / G::C);
-      col_tile<N, COL_FUSED, G::C, true>(v, field, tile, ops, buf, tw, NoHook{});
+      if (LP_BATCH_COL_LEAN && bp->col_lean)
+        col_tile<N, COL_FUSED_LEAN, G::C, true>(v, field, tile, ops, buf, tw, NoHook{});
+      else
+        col_tile<N, COL_FUSED, G::C, true>(v, field, tile, ops, buf, tw, NoHook{});
     } else {
       const int g = threadIdx.x / G::T, t = threadIdx.x % G::T;
       load_row<N, true>(v, field, tile * G::L + g, t);
@@ -285,6 +295,8 @@ lp_status plan_batch(const lp_beam_desc* beams, int count, const lp_batch_option
     r.col = make_colops(b.n, b.area_size, b.wl, b.z, b.z != 0.0,
                         b.flags & (LP_FLAG_PHASE_FP32 | LP_FLAG_EVANESCENT_MASK));
     r.col.scale = 1.0f / ((float)b.n * (float)b.n);
+    r.col_lean = r.col.apply_h && !r.col.phase_fp32 && !r.col.dz && !r.col.kmask &&
+                 !r.col.spectrum_out;
     r.inv = row_ops_none();
     r.inv.iprofile = b.iprofile;
     r.inv.moments = b.moments;
