@@ -35,6 +35,11 @@ using namespace lp;
 #ifndef LP_BATCH_COL_LEAN
 #define LP_BATCH_COL_LEAN 1
 #endif
+// 1: row items run tiles with only the multipliers a batch can carry (a lens
+// in the forward pass, the iprofile and moment epilogues in the inverse).
+#ifndef LP_BATCH_ROW_FEAT
+#define LP_BATCH_ROW_FEAT 1
+#endif
 
 namespace {
 
@@ -101,12 +106,18 @@ __device__ __forceinline__ void run_tiles(const Item& item, const BeamRec* bp, f
     } else {
       const int g = threadIdx.x / G::T, t = threadIdx.x % G::T;
       load_row<N, true>(v, field, tile * G::L + g, t);
+      // plan_batch gives the forward pass at most a lens and the inverse pass
+      // at most the iprofile and moment epilogues (LP_BATCH_ROW_FEAT 0:
+      // kernels with every row multiplier compiled in)
       if (item.pass == 0) {
         const RowOps ops = bp->fwd;
-        row_tile<N, -1, G::L, kBT, true>(v, field, tile, ops, buf, tw, NoHook{});
+        row_tile<N, -1, G::L, kBT, true, 1, NoHook, LP_BATCH_ROW_FEAT ? ROW_LENS : ROW_ALL>(
+            v, field, tile, ops, buf, tw, NoHook{});
       } else {
         const RowOps ops = bp->inv;
-        row_tile<N, 1, G::L, kBT, true>(v, field, tile, ops, buf, tw, NoHook{});
+        row_tile<N, 1, G::L, kBT, true, 1, NoHook,
+                 LP_BATCH_ROW_FEAT ? (ROW_IPROF | ROW_MOMENTS) : ROW_ALL>(v, field, tile, ops, buf,
+                                                                         tw, NoHook{});
       }
     }
   }

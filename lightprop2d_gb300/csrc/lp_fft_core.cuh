@@ -315,15 +315,21 @@ __device__ __forceinline__ void apply_mask_row(float2 (&v)[16], const void* mask
   }
 }
 
+// Row-tile features compiled into a kernel (a bit clear: that part of RowOps
+// is known to be unused, so its code is left out of the kernel).
+constexpr int ROW_LENS = 1, ROW_XMASK = 2, ROW_XSTORE = 4, ROW_SCALE = 8, ROW_IPROF = 16,
+              ROW_MOMENTS = 32;
+constexpr int ROW_ALL = 63, ROW_LEAN = 0;
+
 // Multiply the thread's 16 points of row y by the x-domain multipliers: the
 // lens phase, evaluated in a rolled loop into the thread's own buffer slots
 // (one copy of the phase code), then the mask.  The slots must be free.
-template <int N, int SY = 1>
+template <int N, int SY = 1, int FEAT = ROW_ALL>
 __device__ __forceinline__ void apply_xops(float2 (&v)[16], float2* slots, int nthreads, int y,
                                            int t, const RowOps& ops) {
   constexpr int T = FftGeo<N>::T;
   const int tid = group_tid<SY>();
-  if (ops.lens) {
+  if ((FEAT & ROW_LENS) && ops.lens) {
     const int jy = y - N / 2;
 #pragma unroll 1
     for (int j = 0; j < 16; ++j) {
@@ -337,7 +343,8 @@ __device__ __forceinline__ void apply_xops(float2 (&v)[16], float2* slots, int n
       v[j] = cmul(v[j], slots[j * nthreads + tid]);
     });
   }
-  if (ops.xmask) apply_mask_row<N>(v, ops.xmask, ops.xmask_type, ops.conj, y, t, slots, nthreads, tid);
+  if ((FEAT & ROW_XMASK) && ops.xmask)
+    apply_mask_row<N>(v, ops.xmask, ops.xmask_type, ops.conj, y, t, slots, nthreads, tid);
 }
 
 template <int N, bool CG = false>
@@ -390,12 +397,13 @@ __device__ __forceinline__ void tile_moments(const float2 (&v)[16], int y, int t
 
 // Row tile: rows tile*L .. tile*L+L-1 by the first L*T threads of the
 // exchange group (SY: the CTA, or a 256-thread group), thread (line
-// g = tid / T, t = tid % T).  LEAN: the transform alone (no multipliers,
-// scale or epilogue; the caller checks ops).  v holds the thread's loaded points of row
+// g = tid / T, t = tid % T).  FEAT: the parts of RowOps the kernel supports
+// (ROW_* bits; ROW_LEAN = the transform alone; the caller guarantees that
+// ops uses nothing outside FEAT).  v holds the thread's loaded points of row
 // tile*L + g; `after_first` runs after the first stage (the per-size kernels
 // prefetch the next tile there).  The exchange buffer (L * BUF floats2) must
 // be free on entry.
-template <int N, int S, int L, int NT, bool CG, int SY = 1, class Hook, bool LEAN = false>
+template <int N, int S, int L, int NT, bool CG, int SY = 1, class Hook, int FEAT = ROW_ALL>
 __device__ __forceinline__ void row_tile(float2 (&v)[16], float2* out, int tile, const RowOps& ops,
                                          float2* buf, const float2* tw, Hook after_first) {
   constexpr int T = FftGeo<N>::T;
@@ -403,39 +411,32 @@ __device__ __forceinline__ void row_tile(float2 (&v)[16], float2* out, int tile,
   const int tid = group_tid<SY>();
   const int g = tid / T, t = tid % T;
   const int y = tile * L + g;
-  if constexpr (LEAN) {  // transform only (the caller checked ops)
-    fft_first<N, S, false, L>(v, buf, t, g);
-    after_first();
-    fft_rest<N, S, false, L, LS>(v, buf, tw, t, g);
-    float2* dst = out + (size_t)y * N + t;
-    static_for<16>([&](auto jc) { gst<CG>(dst + T * decltype(jc)::value, v[decltype(jc)::value]); });
-    return;
-  }
-  const bool xops = ops.lens || ops.xmask;
-  if (xops && !ops.x_at_store) {
-    apply_xops<N, SY>(v, buf, NT, y, t, ops);
+  const bool xops = ((FEAT & ROW_LENS) && ops.lens) || ((FEAT & ROW_XMASK) && ops.xmask);
+  const bool at_store = (FEAT & ROW_XSTORE) && ops.x_at_store;
+  if (xops && !at_store) {
+    apply_xops<N, SY, FEAT>(v, buf, NT, y, t, ops);
     group_sync<SY>();
   }
   fft_first<N, S, false, L>(v, buf, t, g);
   after_first();
   fft_rest<N, S, false, L, LS>(v, buf, tw, t, g);
-  if (ops.scale != 1.0f) {
+  if ((FEAT & ROW_SCALE) && ops.scale != 1.0f) {
     static_for<16>([&](auto jc) { v[decltype(jc)::value] = cscale(v[decltype(jc)::value], ops.scale); });
   }
-  if (xops && ops.x_at_store) {
+  if (xops && at_store) {
     group_sync<SY>();
-    apply_xops<N, SY>(v, buf, NT, y, t, ops);
+    apply_xops<N, SY, FEAT>(v, buf, NT, y, t, ops);
   }
   float2* dst = out + (size_t)y * N + t;
   static_for<16>([&](auto jc) { gst<CG>(dst + T * decltype(jc)::value, v[decltype(jc)::value]); });
-  if (ops.iprofile) {
+  if ((FEAT & ROW_IPROF) && ops.iprofile) {
     float* ip = ops.iprofile + (size_t)y * N + t;
     static_for<16>([&](auto jc) {
       constexpr int j = decltype(jc)::value;
       ip[T * j] = fmaf(v[j].x, v[j].x, v[j].y * v[j].y);
     });
   }
-  if constexpr (NT >= 32) {  // whole warps (the batch kernel uses 256 threads)
+  if constexpr (NT >= 32 && (FEAT & ROW_MOMENTS) != 0) {  // whole warps (batch: 256 threads)
     if (ops.moments) tile_moments<N, SY>(v, y, t, ops.moments);
   }
 }

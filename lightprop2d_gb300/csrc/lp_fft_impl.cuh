@@ -162,10 +162,12 @@ __global__ void __launch_bounds__(Geo<N>::ROW_THREADS, LP_ROW_MINB)
     auto pf = [&] {
       if (next < NU) load_row<N>(p, in, next * L + g, t);
     };
-    row_tile<N, S, L, NT, false, 1, decltype(pf), LEAN>(v, out, tile, ops, smem, tw, pf);
+    row_tile<N, S, L, NT, false, 1, decltype(pf), LEAN ? ROW_LEAN : ROW_ALL>(v, out, tile, ops,
+                                                                             smem, tw, pf);
     static_for<16>([&](auto jc) { v[decltype(jc)::value] = p[decltype(jc)::value]; });
 #else
-    row_tile<N, S, L, NT, false, 1, NoHook, LEAN>(v, out, tile, ops, smem, tw, NoHook{});
+    row_tile<N, S, L, NT, false, 1, NoHook, LEAN ? ROW_LEAN : ROW_ALL>(v, out, tile, ops, smem, tw,
+                                                                       NoHook{});
 #endif
     tile = next;
   }
