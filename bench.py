@@ -42,12 +42,12 @@ N_HEAD, AREA, WL, WAIST, Z = 2048, 0.2, 632e-7, 100e-4, 1.0
 # DRAM bytes per launch of the 2048^2 pass kernels, measured with ncu on this
 # workload with caches kept warm between launches (a live step's L2 state):
 # the column pass reads its input from L2 and only writes back evictions.
-NCU_DRAM_BYTES_2048 = {"row_fwd": 58.78e6, "col_fwd_H_inv": 11.18e6, "row_inv": 0.81e6}
+NCU_DRAM_BYTES_2048 = {"row_fwd": 59.22e6, "col_fwd_H_inv": 16.91e6, "row_inv": 0.69e6}
 # The same kernels' FP32 (FMA) pipe and issue activity from an ncu --set full
 # capture of this workload: the FFT passes are bound on-chip, not by DRAM.
-NCU_PIPES_2048 = {"col_fwd_H_inv": {"fma_pipe_active_pct": 33.6, "issue_active_pct": 49.5},
-                  "row_fwd": {"fma_pipe_active_pct": 21.1, "issue_active_pct": 29.7},
-                  "row_inv": {"fma_pipe_active_pct": 21.0, "issue_active_pct": 29.8}}
+NCU_PIPES_2048 = {"col_fwd_H_inv": {"fma_pipe_active_pct": 33.1, "issue_active_pct": 48.4},
+                  "row_fwd": {"fma_pipe_active_pct": 21.5, "issue_active_pct": 30.2},
+                  "row_inv": {"fma_pipe_active_pct": 21.6, "issue_active_pct": 30.3}}
 METRIC = "2048^2 complex64 fused field->field propagates/s"
 UNIT = "propagates/s"
 WORKLOAD = "gaussian beam 2048^2, area 2 mm, wl 632 nm, waist 100 um, complex64, z=1 cm/step"
