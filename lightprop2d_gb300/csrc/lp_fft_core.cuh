@@ -222,13 +222,13 @@ __device__ __forceinline__ void conj16(float2 (&v)[16]) {
 // Multiply the thread's 16 points of row y (columns t + T*j) by an x-domain
 // mask.  The 16 loads are issued before any is used (independent requests
 // in flight); real masks ignore `conj`.
-template <int N>
+template <int N, int MT = -1>
 __device__ __forceinline__ void apply_mask_row(float2 (&v)[16], const void* mask, int type,
                                                int conj, int y, int t, float2* slots,
                                                int nthreads, int tid) {
   constexpr int T = FftGeo<N>::T;
   const size_t row = (size_t)y * N + t;
-  switch (type) {
+  switch (MT >= 0 ? MT : type) {  // MT >= 0: the mask type is known when compiling
     case 1: {  // float32
       const float* p = reinterpret_cast<const float*>(mask) + row;
       float m[16];
@@ -320,11 +320,32 @@ __device__ __forceinline__ void apply_mask_row(float2 (&v)[16], const void* mask
 constexpr int ROW_LENS = 1, ROW_XMASK = 2, ROW_XSTORE = 4, ROW_SCALE = 8, ROW_IPROF = 16,
               ROW_MOMENTS = 32;
 constexpr int ROW_ALL = 63, ROW_LEAN = 0;
+// Row-kernel variants of the per-size passes: every multiplier; the
+// transform alone; an FP32 phase mask (mask type 4) before or after the
+// transform and nothing else (phase-mask design and split-step screens).
+enum RowVariant { ROWV_ALL = 0, ROWV_LEAN = 1, ROWV_PHASE = 2 };
+template <int V>
+constexpr int row_feat() {
+  return V == ROWV_LEAN ? ROW_LEAN : V == ROWV_PHASE ? (ROW_XMASK | ROW_XSTORE) : ROW_ALL;
+}
+template <int V>
+constexpr int row_mask_type() {
+  return V == ROWV_PHASE ? 4 : -1;
+}
+#ifndef LP_ROW_PHASE
+#define LP_ROW_PHASE 1
+#endif
+__host__ __device__ inline int row_variant(const RowOps& o) {
+  const bool plain = !o.lens && o.scale == 1.0f && !o.iprofile && !o.moments;
+  if (plain && !o.xmask) return ROWV_LEAN;
+  if (LP_ROW_PHASE && plain && o.xmask_type == 4) return ROWV_PHASE;
+  return ROWV_ALL;
+}
 
 // Multiply the thread's 16 points of row y by the x-domain multipliers: the
 // lens phase, evaluated in a rolled loop into the thread's own buffer slots
 // (one copy of the phase code), then the mask.  The slots must be free.
-template <int N, int SY = 1, int FEAT = ROW_ALL>
+template <int N, int SY = 1, int FEAT = ROW_ALL, int MT = -1>
 __device__ __forceinline__ void apply_xops(float2 (&v)[16], float2* slots, int nthreads, int y,
                                            int t, const RowOps& ops) {
   constexpr int T = FftGeo<N>::T;
@@ -344,7 +365,7 @@ __device__ __forceinline__ void apply_xops(float2 (&v)[16], float2* slots, int n
     });
   }
   if ((FEAT & ROW_XMASK) && ops.xmask)
-    apply_mask_row<N>(v, ops.xmask, ops.xmask_type, ops.conj, y, t, slots, nthreads, tid);
+    apply_mask_row<N, MT>(v, ops.xmask, ops.xmask_type, ops.conj, y, t, slots, nthreads, tid);
 }
 
 template <int N, bool CG = false>
@@ -403,7 +424,8 @@ __device__ __forceinline__ void tile_moments(const float2 (&v)[16], int y, int t
 // tile*L + g; `after_first` runs after the first stage (the per-size kernels
 // prefetch the next tile there).  The exchange buffer (L * BUF floats2) must
 // be free on entry.
-template <int N, int S, int L, int NT, bool CG, int SY = 1, class Hook, int FEAT = ROW_ALL>
+template <int N, int S, int L, int NT, bool CG, int SY = 1, class Hook, int FEAT = ROW_ALL,
+          int MT = -1>
 __device__ __forceinline__ void row_tile(float2 (&v)[16], float2* out, int tile, const RowOps& ops,
                                          float2* buf, const float2* tw, Hook after_first) {
   constexpr int T = FftGeo<N>::T;
@@ -414,7 +436,7 @@ __device__ __forceinline__ void row_tile(float2 (&v)[16], float2* out, int tile,
   const bool xops = ((FEAT & ROW_LENS) && ops.lens) || ((FEAT & ROW_XMASK) && ops.xmask);
   const bool at_store = (FEAT & ROW_XSTORE) && ops.x_at_store;
   if (xops && !at_store) {
-    apply_xops<N, SY, FEAT>(v, buf, NT, y, t, ops);
+    apply_xops<N, SY, FEAT, MT>(v, buf, NT, y, t, ops);
     group_sync<SY>();
   }
   fft_first<N, S, false, L>(v, buf, t, g);
@@ -425,7 +447,7 @@ __device__ __forceinline__ void row_tile(float2 (&v)[16], float2* out, int tile,
   }
   if (xops && at_store) {
     group_sync<SY>();
-    apply_xops<N, SY, FEAT>(v, buf, NT, y, t, ops);
+    apply_xops<N, SY, FEAT, MT>(v, buf, NT, y, t, ops);
   }
   float2* dst = out + (size_t)y * N + t;
   static_for<16>([&](auto jc) { gst<CG>(dst + T * decltype(jc)::value, v[decltype(jc)::value]); });

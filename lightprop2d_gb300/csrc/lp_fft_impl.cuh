@@ -7,6 +7,13 @@
 // arithmetic.  Stage twiddles are copied into shared memory once per CTA.
 // Launches use programmatic dependent launch so the next pass's CTAs are
 // scheduled as this pass retires.
+//
+// Each pass exists in a general form (every multiplier a run-time option)
+// and in forms compiled for what most calls use: the row transform alone, a
+// row pass with only an FP32 phase mask, and column passes whose only
+// spectral multiplier is H.  The launchers pick by the call's ops; the
+// specialised kernels leave the unused code out, which removes the general
+// column kernel's instruction-cache stalls.
 #pragma once
 
 #include "lp_async.cuh"
@@ -134,7 +141,7 @@ __device__ __forceinline__ void load_twiddles(float2* dst) {
   for (int i = threadIdx.x; i < FftGeo<LP_N>::TW_SIZE; i += NT) dst[i] = g_tw[i];
 }
 
-template <int N, int S, bool LEAN = false>
+template <int N, int S, int V = ROWV_ALL>
 __global__ void __launch_bounds__(Geo<N>::ROW_THREADS, LP_ROW_MINB)
     row_kernel(const float2* in, float2* out, RowOps ops) {
   constexpr int T = Geo<N>::T, L = Geo<N>::ROWS, NU = Geo<N>::ROW_UNITS;
@@ -162,12 +169,12 @@ __global__ void __launch_bounds__(Geo<N>::ROW_THREADS, LP_ROW_MINB)
     auto pf = [&] {
       if (next < NU) load_row<N>(p, in, next * L + g, t);
     };
-    row_tile<N, S, L, NT, false, 1, decltype(pf), LEAN ? ROW_LEAN : ROW_ALL>(v, out, tile, ops,
-                                                                             smem, tw, pf);
+    row_tile<N, S, L, NT, false, 1, decltype(pf), row_feat<V>(), row_mask_type<V>()>(
+        v, out, tile, ops, smem, tw, pf);
     static_for<16>([&](auto jc) { v[decltype(jc)::value] = p[decltype(jc)::value]; });
 #else
-    row_tile<N, S, L, NT, false, 1, NoHook, LEAN ? ROW_LEAN : ROW_ALL>(v, out, tile, ops, smem, tw,
-                                                                       NoHook{});
+    row_tile<N, S, L, NT, false, 1, NoHook, row_feat<V>(), row_mask_type<V>()>(
+        v, out, tile, ops, smem, tw, NoHook{});
 #endif
     tile = next;
   }
@@ -329,7 +336,7 @@ struct RowTma {
   static constexpr size_t SMEM = BAR_BYTES + G * SL * sizeof(uint64_t);
 };
 
-template <int N, int S>
+template <int N, int S, int V = ROWV_ALL>
 __global__ void __launch_bounds__(512, 1)
     row_kernel_tma(const float2* in, float2* out, RowOps ops, int tpg) {
   using RT = RowTma<N>;
@@ -377,7 +384,8 @@ __global__ void __launch_bounds__(512, 1)
       fence_proxy_async();
       bulk_load(land + k * TILE, in + (size_t)(first + (j + SL) * step) * TILE, BYTES, bars + k);
     }
-    row_tile<N, S, L, 256, false, 2>(v, out, first + j * step, ops, xbuf, tw, NoHook{});
+    row_tile<N, S, L, 256, false, 2, NoHook, row_feat<V>(), row_mask_type<V>()>(
+        v, out, first + j * step, ops, xbuf, tw, NoHook{});
   }
   if (!ok && lt == 0) {
     // A wait gave up: let each slot's last copy land (bounded) before exit.
@@ -440,12 +448,12 @@ cudaError_t init_size() {
 #if LP_ROW_TMA_SIZE
   {
     const int ts = (int)RowTma<N>::SMEM;
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(row_kernel_tma<N, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               ts);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(row_kernel_tma<N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               ts);
+    for (const void* k : {(const void*)row_kernel_tma<N, -1>, (const void*)row_kernel_tma<N, 1>,
+                          (const void*)row_kernel_tma<N, -1, ROWV_LEAN>,
+                          (const void*)row_kernel_tma<N, 1, ROWV_LEAN>,
+                          (const void*)row_kernel_tma<N, -1, ROWV_PHASE>,
+                          (const void*)row_kernel_tma<N, 1, ROWV_PHASE>})
+      if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, ts);
   }
 #endif
 #if LP_COL_TMA
@@ -472,10 +480,11 @@ cudaError_t init_size() {
                              cudaFuncAttributeMaxDynamicSharedMemorySize, cs);
 #endif
 #if LP_ROW_LEAN
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(row_kernel<N, -1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(row_kernel<N, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, rs);
+  for (const void* k : {(const void*)row_kernel<N, -1, ROWV_LEAN>,
+                        (const void*)row_kernel<N, 1, ROWV_LEAN>,
+                        (const void*)row_kernel<N, -1, ROWV_PHASE>,
+                        (const void*)row_kernel<N, 1, ROWV_PHASE>})
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, rs);
 #endif
 #if LP_CARVEOUT >= 0
   for (const void* k : {(const void*)row_kernel<N, -1>, (const void*)row_kernel<N, 1>,
@@ -514,19 +523,27 @@ cudaError_t launch_row(int inverse, const float2* in, float2* out, const RowOps&
       const int tpg = (RT::NU + RT::G * g_sms - 1) / (RT::G * g_sms);
       const int grid = LP_TMA_BALANCED ? (RT::NU + RT::G * tpg - 1) / (RT::G * tpg)
                                        : cmin(g_sms, (RT::NU + RT::G - 1) / RT::G);
-      return launch_pdl(inverse ? row_kernel_tma<N, 1> : row_kernel_tma<N, -1>, grid, 512,
-                        RT::SMEM, st, in, out, ops, tpg);
+      const int v = LP_ROW_LEAN ? row_variant(ops) : ROWV_ALL;
+      auto k = inverse ? (v == ROWV_LEAN    ? row_kernel_tma<N, 1, ROWV_LEAN>
+                          : v == ROWV_PHASE ? row_kernel_tma<N, 1, ROWV_PHASE>
+                                            : row_kernel_tma<N, 1>)
+                       : (v == ROWV_LEAN    ? row_kernel_tma<N, -1, ROWV_LEAN>
+                          : v == ROWV_PHASE ? row_kernel_tma<N, -1, ROWV_PHASE>
+                                            : row_kernel_tma<N, -1>);
+      return launch_pdl(k, grid, 512, RT::SMEM, st, in, out, ops, tpg);
     }
   }
 #endif
   const int grid = grid_for(Geo<N>::ROW_UNITS, g_occ_row, g_ctas_row);
 #if LP_ROW_LEAN
-  if (!ops.lens && !ops.xmask && ops.scale == 1.0f && !ops.iprofile && !ops.moments) {
-    if (inverse)
-      return launch_pdl(row_kernel<N, 1, true>, grid, Geo<N>::ROW_THREADS, Geo<N>::ROW_SMEM, st,
-                        in, out, ops);
-    return launch_pdl(row_kernel<N, -1, true>, grid, Geo<N>::ROW_THREADS, Geo<N>::ROW_SMEM, st,
-                      in, out, ops);
+  {
+    const int v = row_variant(ops);
+    if (v != ROWV_ALL) {
+      auto k = inverse ? (v == ROWV_LEAN ? row_kernel<N, 1, ROWV_LEAN> : row_kernel<N, 1, ROWV_PHASE>)
+                       : (v == ROWV_LEAN ? row_kernel<N, -1, ROWV_LEAN>
+                                         : row_kernel<N, -1, ROWV_PHASE>);
+      return launch_pdl(k, grid, Geo<N>::ROW_THREADS, Geo<N>::ROW_SMEM, st, in, out, ops);
+    }
   }
 #endif
   if (inverse)

@@ -278,3 +278,45 @@ def test_errors_are_raised(B):
         B.fft2(torch.zeros((64, 64), dtype=torch.float32, device="cuda"))  # not complex
     with pytest.raises(ValueError):
         B.propagate(torch.zeros((64, 64), dtype=torch.complex64, device="cuda"), -1.0, 1e-4, 1.0)
+
+
+@pytest.mark.parametrize("n", [256, 1024, 2048, 4096])
+def test_specialised_and_general_kernels_agree(B, n):
+    """The launcher runs kernels compiled for what a call uses: transform-only
+    row passes and an H-only column pass when there is no multiplier, an
+    FP32-phase-mask row pass for a phase mask alone.  Adding a multiplier of
+    value one (an all-ones k mask, an iprofile epilogue) sends the same call
+    through the general kernels; both must match the oracle and each other."""
+    from lightprop2d_gb300 import _lib as L
+    area, wl, z = 1 * mm, 632 * nm, 1.3
+    g = O.grids(area, n, wl)
+    x = rand_field(n, 5 * n + 1)
+    _, f_ref = O.propagate(np.fft.fft2(x), g["Kz"], z)
+    ones = torch.ones((n, n), dtype=torch.float32, device="cuda")
+    lean = host(B.propagate_field(dev(x), area, wl, z))
+    ip = torch.empty((n, n), dtype=torch.float32, device="cuda")
+    general = host(B.propagate_field(dev(x), area, wl, z, kmask=ones, iprofile_out=ip))
+    assert O.rel_l2(lean, f_ref) < TOL
+    assert O.rel_l2(general, f_ref) < TOL
+    assert O.rel_l2(lean, general) < 1e-6
+    # FP32 phase mask alone (before and after the transform) vs with an epilogue
+    rng = np.random.default_rng(n)
+    phi = rng.uniform(-20.0, 20.0, (n, n)).astype(np.float32)
+    pm = torch.as_tensor(phi, device="cuda")
+    mult = np.exp(1j * phi.astype(np.float64))
+    _, ref_before = O.propagate(np.fft.fft2(x * mult), g["Kz"], z)
+    cm = torch.as_tensor(mult.astype(np.complex64), device="cuda")
+    # before the transform: the phase-mask row kernel vs a complex64 mask of
+    # the same values (general kernel); after it: alone vs with an epilogue
+    a = host(B.propagate_field(dev(x), area, wl, z, xmask=pm, xmask_phase=True))
+    b = host(B.propagate_field(dev(x), area, wl, z, xmask=cm))
+    assert O.rel_l2(a, ref_before) < TOL
+    assert O.rel_l2(b, ref_before) < TOL
+    assert O.rel_l2(a, b) < 2e-6
+    after = L.LP_FLAG_XMASK_AFTER
+    a = host(B.propagate_field(dev(x), area, wl, z, xmask=pm, xmask_phase=True, flags=after))
+    b = host(B.propagate_field(dev(x), area, wl, z, xmask=pm, xmask_phase=True, flags=after,
+                               iprofile_out=ip))
+    assert O.rel_l2(a, f_ref * mult) < TOL
+    assert O.rel_l2(b, f_ref * mult) < TOL
+    assert O.rel_l2(a, b) < 1e-6
