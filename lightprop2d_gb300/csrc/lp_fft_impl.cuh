@@ -23,9 +23,11 @@
 #error "define LP_N before including lp_fft_impl.cuh"
 #endif
 // Columns per CTA of the column kernels for N = 1024, 2048 and 4096 (2048:
-// eight columns, 1024 threads, measured 41.0 vs 42.2 us against four; 4096:
-// four columns, 1024 threads without prefetch, 155.8 vs 192.9 us against two
-// columns with prefetch).
+// eight columns, 1024 threads, measured 41.0 vs 42.2 us against four, 41.7
+// us for two four-column CTAs per SM and 43.6 us for seven-column tiles,
+// which even out the SMs' work but not a tile's latency; 4096: four
+// columns, 1024 threads without prefetch, 155.8 vs 192.9 us against two
+// columns with prefetch and 222 us for two two-column CTAs per SM).
 #ifndef LP_COL_C1024
 #define LP_COL_C1024 4
 #endif
@@ -46,6 +48,12 @@
 // current one; 0: load it at the top of the next iteration.
 #ifndef LP_ROW_PREFETCH
 #define LP_ROW_PREFETCH (LP_N < 8192 && LP_N != 1024)
+#endif
+// Rows loaded ahead by the transform-only row kernel (0, 1 or 2; measured:
+// two rows ahead at 2048^2 57.2 vs 56.6 us per propagate, one row ahead at
+// 1024^2 18.1 vs 17.9 us).
+#ifndef LP_ROW_PREFETCH_LEAN
+#define LP_ROW_PREFETCH_LEAN LP_ROW_PREFETCH
 #endif
 #ifndef LP_COL_PREFETCH
 #define LP_COL_PREFETCH 0
@@ -152,31 +160,39 @@ __global__ void __launch_bounds__(Geo<N>::ROW_THREADS, LP_ROW_MINB)
   load_twiddles<NT>(tw);
   pdl_wait();
   pdl_release();
+  // rows loaded ahead of the one being transformed (0: none)
+  constexpr int PF = (V == ROWV_LEAN) ? LP_ROW_PREFETCH_LEAN : LP_ROW_PREFETCH;
   int tile = blockIdx.x;
-  float2 v[16];
-#if LP_ROW_PREFETCH
-  float2 p[16];
-  if (tile < NU) load_row<N>(v, in, tile * L + g, t);
-#endif
+  const int step = gridDim.x;
+  float2 v[16], p[PF >= 1 ? 16 : 1], q[PF >= 2 ? 16 : 1];
+  if constexpr (PF >= 1) {
+    if (tile < NU) load_row<N>(v, in, tile * L + g, t);
+  }
+  if constexpr (PF >= 2) {
+    if (tile + step < NU) load_row<N>(p, in, (tile + step) * L + g, t);
+  }
 #pragma unroll 1
   while (tile < NU) {
-    const int next = tile + gridDim.x;
-#if !LP_ROW_PREFETCH
-    load_row<N>(v, in, tile * L + g, t);
-#endif
+    if constexpr (PF == 0) load_row<N>(v, in, tile * L + g, t);
     __syncthreads();  // buffer free: previous tile's last-stage reads are done
-#if LP_ROW_PREFETCH
-    auto pf = [&] {
-      if (next < NU) load_row<N>(p, in, next * L + g, t);
-    };
-    row_tile<N, S, L, NT, false, 1, decltype(pf), row_feat<V>(), row_mask_type<V>()>(
-        v, out, tile, ops, smem, tw, pf);
-    static_for<16>([&](auto jc) { v[decltype(jc)::value] = p[decltype(jc)::value]; });
-#else
-    row_tile<N, S, L, NT, false, 1, NoHook, row_feat<V>(), row_mask_type<V>()>(
-        v, out, tile, ops, smem, tw, NoHook{});
-#endif
-    tile = next;
+    if constexpr (PF == 0) {
+      row_tile<N, S, L, NT, false, 1, NoHook, row_feat<V>(), row_mask_type<V>()>(
+          v, out, tile, ops, smem, tw, NoHook{});
+    } else {
+      const int ahead = tile + PF * step;
+      auto pf = [&] {
+        if (ahead < NU) {
+          if constexpr (PF == 1) load_row<N>(p, in, ahead * L + g, t);
+          else load_row<N>(q, in, ahead * L + g, t);
+        }
+      };
+      row_tile<N, S, L, NT, false, 1, decltype(pf), row_feat<V>(), row_mask_type<V>()>(
+          v, out, tile, ops, smem, tw, pf);
+      static_for<16>([&](auto jc) { v[decltype(jc)::value] = p[decltype(jc)::value]; });
+      if constexpr (PF >= 2)
+        static_for<16>([&](auto jc) { p[decltype(jc)::value] = q[decltype(jc)::value]; });
+    }
+    tile += step;
   }
 }
 
