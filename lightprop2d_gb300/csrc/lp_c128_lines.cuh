@@ -445,12 +445,25 @@ enum ZMode { Z_FWD = 0, Z_INV = 1, Z_FUSED = 2, Z_KINV = 3 };
 // index = ky): k multipliers, [spectrum write], inverse.  IN_D / OUT_D: the pass reads / writes
 // complex128 (else float-float intermediates).
 // Lines per CTA of a pass: column passes take at least two adjacent columns.
-template <int N, bool COLS>
-using ZG = ZGeo<N, COLS ? 2 : 1>;
+// 1: the k-first row pass (Z_KINV) takes rows ky and N - ky in one CTA and
+// evaluates their common H (Ky**2 is the same) once.
+#ifndef LP_ZKINV_PAIRS
+#define LP_ZKINV_PAIRS 1
+#endif
+template <int N, int MODE, bool COLS>
+constexpr bool zpairs() {
+  // N <= 2048: two rows in at most 512 threads (measured at 2048^2: 0.256 vs
+  // 0.290 ms per spectrum-state propagate; 4096 would need 1024-thread CTAs)
+  return LP_ZKINV_PAIRS && MODE == Z_KINV && !COLS && ZGeo<N>::TL <= 256;
+}
+// Geometry of a pass: at least two lines per CTA for column passes and for
+// the paired k-first row pass.
+template <int N, int MODE, bool COLS>
+using ZGM = ZGeo<N, (COLS || zpairs<N, MODE, COLS>()) ? 2 : 1>;
 
 template <int N, int MODE, bool COLS>
 constexpr int zmin_blocks() {
-  constexpr int nt = ZG<N, COLS>::NT;
+  constexpr int nt = ZGM<N, MODE, COLS>::NT;
   // 64 registers (four CTAs a SM) for the plain passes; the passes with H
   // or lens tables take 85 (three)
   constexpr bool tables = MODE >= Z_FUSED || (MODE == Z_FWD && !COLS);
@@ -468,34 +481,46 @@ constexpr int zmin_blocks() {
 // line index = ky): k multipliers, [spectrum write], inverse.  IN_D / OUT_D:
 // the pass reads / writes complex128 (else float-float intermediates).
 template <int N, int MODE, bool IN_D, bool OUT_D, bool COLS>
-__global__ void __launch_bounds__(ZG<N, COLS>::NT, zmin_blocks<N, MODE, COLS>())
+__global__ void __launch_bounds__(ZGM<N, MODE, COLS>::NT, zmin_blocks<N, MODE, COLS>())
     zline_kernel(const void* __restrict__ in, void* out, ZOps o, const zf* __restrict__ tw) {
-  using G = ZG<N, COLS>;
+  using G = ZGM<N, MODE, COLS>;
+  constexpr bool PAIRS = zpairs<N, MODE, COLS>();
   constexpr int LS = COLS ? G::L : 1;  // element stride of a line in shared memory
   extern __shared__ float4 zs[];
   const int g = COLS ? (int)(threadIdx.x % G::L) : (int)(threadIdx.x / G::TL);
   const int t = COLS ? (int)(threadIdx.x / G::L) : (int)(threadIdx.x % G::TL);
-  const int line = blockIdx.x * G::L + g;
+  // PAIRS: lines g = 2p, 2p + 1 of the CTA are rows b and N - b of pair
+  // base b = blockIdx.x * L/2 + p (b = 0 .. N/2; rows 0 and N/2 are their
+  // own mirrors, so the second line of those pairs is idle)
+  const int pb = (int)blockIdx.x * (G::L / 2) + g / 2;
+  const int line = PAIRS ? ((g & 1) ? N - pb : pb) : (int)blockIdx.x * G::L + g;
   zf* buf = COLS ? zs + g : zs + (size_t)g * N;
   // grid offset of element x of this line
   auto at = [&](int x) -> size_t {
     return COLS ? (size_t)x * N + line : (size_t)line * N + x;
   };
-  const bool live = line < N;  // N < L: a CTA has more line slots than lines
+  // N < L: a CTA has more line slots than lines
+  const bool live = PAIRS ? ((g & 1) ? (pb >= 1 && pb < N / 2) : pb <= N / 2) : line < N;
   if constexpr (MODE == Z_KINV) {
     // H of this row (ky = line) at |kx| = 0..N/2 once each (H(kx, ky) =
-    // H(-kx, ky)), filled while the row's loads are in flight
+    // H(-kx, ky)), filled while the row's loads are in flight; with PAIRS one
+    // table serves rows ky and N - ky and both rows' threads fill it
     zf v[G::PT];
 #pragma unroll
     for (int i = 0; i < G::PT && i * G::TL < N; ++i)
       v[i] = live ? z2_to_zf(reinterpret_cast<const z2*>(in)[at(t + G::TL * i)])
                   : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    zf* hb = zs + (size_t)G::L * N + (size_t)g * G::HT;
+    zf* hb = zs + (size_t)G::L * N + (size_t)(PAIRS ? g / 2 : g) * G::HT;
     if (o.apply_h) {
       const int h = (N + 1) / 2;
-      const double fy = (double)(line < h ? line : line - N) * o.val;
+      const int ky = PAIRS ? pb : line;  // Ky**2 of row N - b equals that of row b
+      const double fy = (double)(ky < h ? ky : ky - N) * o.val;
       const double fy2 = fy * fy;
-      for (int j = t; j < G::HT; j += G::TL) hb[j] = zh_value_kx(o, fy2, j);
+      if constexpr (PAIRS) {
+        for (int j = t + (g & 1) * G::TL; j < G::HT; j += 2 * G::TL) hb[j] = zh_value_kx(o, fy2, j);
+      } else {
+        for (int j = t; j < G::HT; j += G::TL) hb[j] = zh_value_kx(o, fy2, j);
+      }
     }
     __syncthreads();
 #pragma unroll
@@ -624,8 +649,17 @@ __global__ void __launch_bounds__(ZG<N, COLS>::NT, zmin_blocks<N, MODE, COLS>())
 // passes) or the lens tables (first row pass).
 template <int N, int M, bool I, bool C>
 constexpr size_t zsmem_bytes() {
-  using G = ZG<N, C>;
+  using G = ZGM<N, M, C>;
+  if constexpr (zpairs<N, M, C>()) return 16 * ((size_t)G::L * N + (size_t)(G::L / 2) * G::HT);
   return M >= Z_FUSED ? G::SMEM_FUSED : (M == Z_FWD && !C && I) ? G::SMEM_FWD : G::SMEM;
+}
+
+// CTAs of a pass: N / L lines, or N/2 + 1 row pairs for the paired pass.
+template <int N, int M, bool C>
+constexpr int zgrid() {
+  using G = ZGM<N, M, C>;
+  if constexpr (zpairs<N, M, C>()) return (N / 2 + 1 + G::L / 2 - 1) / (G::L / 2);
+  return (N + G::L - 1) / G::L;
 }
 
 template <int N>
@@ -653,8 +687,8 @@ cudaError_t zline(int mode, bool in_d, bool out_d, bool cols, const void* in, vo
   bool done = false;
 #define LP_ZLAUNCH(M, I, O, C)                                                              \
   if (!done && mode == M && in_d == I && out_d == O && cols == C) {                         \
-    using G = ZG<N, C>;                                                                     \
-    zline_kernel<N, M, I, O, C><<<(N + G::L - 1) / G::L, G::NT, zsmem_bytes<N, M, I, C>(),  \
+    using G = ZGM<N, M, C>;                                                                 \
+    zline_kernel<N, M, I, O, C><<<zgrid<N, M, C>(), G::NT, zsmem_bytes<N, M, I, C>(),      \
                                   st>>>(in, out, o, tw);                                    \
     done = true;                                                                            \
   }
