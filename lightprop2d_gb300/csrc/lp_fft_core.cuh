@@ -25,6 +25,7 @@
 
 #include <cmath>
 
+#include "lightprop2d_gb300.h"
 #include "lp_device.cuh"
 #include "lp_internal.h"
 
@@ -323,6 +324,7 @@ constexpr int ROW_ALL = 63, ROW_LEAN = 0;
 // Row-kernel variants of the per-size passes: every multiplier; the
 // transform alone; an FP32 phase mask (mask type 4) before or after the
 // transform and nothing else (phase-mask design and split-step screens).
+static_assert(LP_MASK_PHASE_F32 == 4, "apply_mask_row's case 4 is the FP32 phase mask");
 enum RowVariant { ROWV_ALL = 0, ROWV_LEAN = 1, ROWV_PHASE = 2 };
 template <int V>
 constexpr int row_feat() {
@@ -330,7 +332,7 @@ constexpr int row_feat() {
 }
 template <int V>
 constexpr int row_mask_type() {
-  return V == ROWV_PHASE ? 4 : -1;
+  return V == ROWV_PHASE ? (int)LP_MASK_PHASE_F32 : -1;
 }
 #ifndef LP_ROW_PHASE
 #define LP_ROW_PHASE 1
@@ -338,7 +340,7 @@ constexpr int row_mask_type() {
 __host__ __device__ inline int row_variant(const RowOps& o) {
   const bool plain = !o.lens && o.scale == 1.0f && !o.iprofile && !o.moments;
   if (plain && !o.xmask) return ROWV_LEAN;
-  if (LP_ROW_PHASE && plain && o.xmask_type == 4) return ROWV_PHASE;
+  if (LP_ROW_PHASE && plain && o.xmask_type == LP_MASK_PHASE_F32) return ROWV_PHASE;
   return ROWV_ALL;
 }
 
